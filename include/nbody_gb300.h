@@ -1,0 +1,190 @@
+/*
+ * nbody_gb300.h -- C ABI of the GB300 (sm_103a) all-pairs gravity library.
+ *
+ * Plain pointers and sizes only.  Streams are passed as `void *` holding a
+ * cudaStream_t (NULL = the legacy default stream).  Device pointers must be
+ * 16-byte aligned (float4 arrays); workspaces 256-byte aligned.
+ *
+ * Layouts follow the reference (src/nbody.cu:127-156):
+ *   posMass     float4 {x, y, z, m}
+ *   velInvMass  float4 {vx, vy, vz, 1/m}
+ *   force       float4 {fx, fy, fz, w}; the sum carries m_j but not m_i or G,
+ *               i.e. it is the acceleration (src/bodybodyInteraction.cuh:40-65)
+ */
+#ifndef NBODY_GB300_H
+#define NBODY_GB300_H
+
+#include <stddef.h>
+
+#include "nbgb_status.h"
+
+#define NBGB_API __attribute__((visibility("default")))
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ======================================================================== */
+/* Drop-in algorithm entry point                                             */
+/* ======================================================================== */
+
+/*
+ * Replaces: pfnComputeGravitation_AOS_t (src/nbody.h:68), i.e. one more row
+ * of s_algorithms[] (src/nbody.cu:83-103) of type ALGORITHM_AOS_GPU, like
+ * ComputeGravitation_GPU_Shared (src/nbody_GPU_Shared.cu:83-103).
+ *
+ * force, posMass: DEVICE pointers to N float4 each (the driver's
+ * g_dptrAOS_Force / g_dptrAOS_PosMass, src/nbody.cu:351-370).  Writes
+ * force[i].xyz and sets force[i].w = 0.  Any N >= 1 is accepted (the
+ * reference driver always passes a multiple of 1024).
+ *
+ * Runs on the legacy default stream, synchronises the device before
+ * returning, and returns the elapsed milliseconds measured by CUDA events
+ * around its launches; returns 0 on any error, which the reference driver
+ * treats as "skip this algorithm" (src/nbody.cu:385-386).  Scratch space is
+ * allocated on first use and cached per device (nbgb_release_workspace frees
+ * it).  Not re-entrant across host threads on the same device.
+ */
+NBGB_API float ComputeGravitation_GPU_GB300(float *force, float *posMass, float softeningSquared,
+                                            size_t N);
+
+/* Frees the drop-in entry point's cached scratch space on every device. */
+NBGB_API void nbgb_release_workspace(void);
+
+/* ======================================================================== */
+/* Stream-ordered force evaluation with a caller-owned workspace             */
+/* ======================================================================== */
+
+/* Workspace bytes nbgb_force needs for N bodies on the current device
+   (0 if N is unsupported). */
+NBGB_API size_t nbgb_force_workspace_bytes(size_t N);
+
+/*
+ * Same sum as ComputeGravitation_GPU_GB300 (replaces the kernel launch inside
+ * the reference's GPU algorithms, e.g. src/nbody_GPU_Shared.cu:91-95), but
+ * asynchronous on `stream`, with scratch in a caller-provided DEVICE
+ * workspace of at least nbgb_force_workspace_bytes(N) bytes.  Returns
+ * NBGB_OK or a negative NBGB_ERR_* code; device-side failures are reported by
+ * nbgb_last_status after the stream is synchronised.  Calls that share a
+ * workspace must not overlap on the GPU.
+ */
+NBGB_API int nbgb_force(float *force, const float *posMass, float softeningSquared, size_t N,
+                        void *workspace, size_t workspace_bytes, void *stream);
+
+/* As nbgb_force with the kernel configuration and j-split forced (-1 = the
+   planner's choice).  For tests and tuning. */
+NBGB_API int nbgb_force_ex(float *force, const float *posMass, float softeningSquared, size_t N,
+                           void *workspace, size_t workspace_bytes, int config, int nsplit,
+                           void *stream);
+
+/* The planner's decision for N (config / nsplit forced when >= 0). */
+NBGB_API int nbgb_force_plan(size_t N, int config, int nsplit, int *out_config, int *out_nsplit,
+                             size_t *out_workspace_bytes);
+NBGB_API int nbgb_force_num_configs(void);
+NBGB_API const char *nbgb_force_config_name(int config);
+
+/* ======================================================================== */
+/* Integration step                                                          */
+/* ======================================================================== */
+
+/*
+ * Replaces: integrateGravitation_SOA / integrateOne (src/nbody.cu:158-236),
+ * which the reference runs on one host thread.  DEVICE float4 arrays, in
+ * place: v += (F * invMass) * dt; v *= damping; x += v * dt, each operation
+ * rounded separately in binary32 (bit-identical to IEEE single precision
+ * evaluation of that formula on the host).  posMass.w and velInvMass.w are
+ * preserved.  Asynchronous on `stream`.
+ */
+NBGB_API int nbgb_integrate_reference(float *posMass, float *velInvMass, const float *force,
+                                      float dt, float damping, size_t N, void *stream);
+
+/* ======================================================================== */
+/* Device-resident simulation (the reference's per-step orchestration,      */
+/* src/nbody.cu:293-470, without host copies)                               */
+/* ======================================================================== */
+
+#define NBGB_INTEGRATOR_REFERENCE 0 /* integrateOne, FP32, damping        */
+#define NBGB_INTEGRATOR_KDK64 1     /* FP64 kick-drift-kick, a = F         */
+
+typedef struct nbgb_system nbgb_system;
+
+/* Allocates all device state on the current device; NULL on failure. */
+NBGB_API nbgb_system *nbgb_system_create(size_t N, int integrator, float softeningSquared,
+                                         float dt, float damping);
+NBGB_API void nbgb_system_destroy(nbgb_system *sys);
+/* HOST float4 arrays in (posMass, velInvMass). */
+NBGB_API int nbgb_system_set_state(nbgb_system *sys, const float *posMass,
+                                   const float *velInvMass);
+/* KDK only: HOST double[N][3] positions and velocities, float[N] masses. */
+NBGB_API int nbgb_system_set_state64(nbgb_system *sys, const double *pos3, const double *vel3,
+                                     const float *mass);
+/* Advance nsteps (asynchronous; reference steps replay one CUDA graph). */
+NBGB_API int nbgb_system_step(nbgb_system *sys, int nsteps);
+NBGB_API int nbgb_system_set_graph(nbgb_system *sys, int enable);
+/* Bracket every force launch with CUDA events on the system's stream (steps
+   then run eagerly); nbgb_system_last_force_ms reads the latest one. */
+NBGB_API int nbgb_system_set_timing(nbgb_system *sys, int enable);
+NBGB_API int nbgb_system_last_force_ms(nbgb_system *sys, float *ms);
+NBGB_API int nbgb_system_synchronize(nbgb_system *sys);
+/* HOST float4 arrays out (either may be NULL); synchronises. */
+NBGB_API int nbgb_system_get_state(nbgb_system *sys, float *posMass, float *velInvMass);
+NBGB_API int nbgb_system_get_state64(nbgb_system *sys, double *pos3, double *vel3);
+/* Forces of the most recent force pass, HOST float4; synchronises. */
+NBGB_API int nbgb_system_get_force(nbgb_system *sys, float *force);
+NBGB_API void *nbgb_system_device_posmass(nbgb_system *sys);
+NBGB_API void *nbgb_system_device_force(nbgb_system *sys);
+NBGB_API void *nbgb_system_stream(nbgb_system *sys);
+NBGB_API int nbgb_system_plan(nbgb_system *sys, int *config, int *nsplit);
+
+/* ======================================================================== */
+/* Initial conditions and error statistics (host)                            */
+/* ======================================================================== */
+
+/* Replaces: seedRandom + randomUnitBodies (src/nbody_util.cpp:81-144) as the
+   driver calls them (src/nbody.cu:919, 996; scale 0.9, velscale 8): same LCG,
+   same rejection order, so equal seeds give equal bodies.  HOST float4. */
+NBGB_API int nbgb_ic_reference(float *posMass, float *velInvMass, size_t N, float scale,
+                               float velscale, unsigned seed);
+/* Uniform ball of the given radius, masses U[m_lo, m_hi] / N, zero
+   velocities (velInvMass may be NULL).  HOST float4. */
+NBGB_API int nbgb_ic_uniform_ball(float *posMass, float *velInvMass, size_t N, double radius,
+                                  double m_lo, double m_hi, unsigned long long seed);
+/* Plummer sphere (G = M = a = 1, equal masses, virial velocities).  Any of
+   the FP64 double[N][3] or FP32 float4 outputs may be NULL. */
+NBGB_API int nbgb_ic_plummer(double *pos3, double *vel3, float *posMass, float *velInvMass,
+                             size_t N, unsigned long long seed);
+
+/* Replaces: the crosscheck loop (src/nbody.cu:120-125, 406-418): max over
+   bodies and x,y,z of |a - b| / b (signed b).  HOST float4. */
+NBGB_API float nbgb_crosscheck_max_rel_error(const float *force, const float *golden, size_t N);
+/* Per-body |F - T| / |T| against FP64 truth double[n_rows][3]; row t is body
+   idx[t] (idx NULL: body t).  Max and RMS over rows. */
+NBGB_API int nbgb_force_error_stats(const float *force, const double *truth3,
+                                    const long long *idx, size_t n_rows, double *max_rel,
+                                    double *rms_rel);
+
+/* ======================================================================== */
+/* Pipe-throughput microbenchmarks (roofline denominators)                   */
+/* ======================================================================== */
+
+/* which: 0 = scalar FP32 FMA (FLOP/s, FMA = 2), 1 = packed f32x2 FMA
+   (FLOP/s), 2 = MUFU rsqrt (results/s).  Full-GPU launch of `iters` x 128
+   operations per thread, best of `reps` after a warm-up.  Synchronous. */
+NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms);
+
+/* ======================================================================== */
+/* Status                                                                    */
+/* ======================================================================== */
+
+/* Reads and clears the device status word of the current device (bits
+   NBGB_STATUS_*).  Returns the bits, or a negative NBGB_ERR_* code. */
+NBGB_API int nbgb_last_status(void);
+NBGB_API const char *nbgb_status_string(int code);
+/* Library / build identification. */
+NBGB_API const char *nbgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBODY_GB300_H */

@@ -1,0 +1,311 @@
+"""GB300 (sm_103a) all-pairs softened gravity: Python mirror of the C ABI.
+
+The reference (tycho/nbody) exposes its force path as rows of an algorithm
+table, `float (*)(float *force, float *posMass, float softeningSquared,
+size_t N)` (src/nbody.h:68), driven once per step by ComputeGravitation()
+(src/nbody.cu:293-470), which integrates on the host with integrateOne
+(src/nbody.cu:158-182).  This package keeps those names and meanings:
+
+  ComputeGravitation_GPU_GB300(force, posMass, softeningSquared, N) -> ms
+      the drop-in algorithm row (device pointers, returns ms, 0 on error)
+  force(posMass, softeningSquared)          stream-ordered force on tensors
+  integrate_reference(posMass, velInvMass, force, dt, damping)
+      integrateOne on the GPU, bit-identical to its IEEE binary32 evaluation
+  System(N, ...)                            device-resident step loop
+  ic_reference / ic_uniform_ball / ic_plummer   initial conditions
+  crosscheck_max_rel_error                  the reference's crosscheck metric
+
+All compute runs in libnbody_gb300.so; there is no CPU fallback.  PyTorch is
+used only for device memory and streams.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import LIB_PATH, NbgbError, check, load  # noqa: F401
+
+INTEGRATOR_REFERENCE = 0
+INTEGRATOR_KDK64 = 1
+
+# Reference driver constants (src/nbody.cu:80-81, 151-156).
+REFERENCE_SOFTENING = 0.1
+REFERENCE_DAMPING = 0.95
+REFERENCE_TIMESTEP = 0.016
+REFERENCE_SCALE = 0.9
+REFERENCE_VELOCITY_SCALE = 8.0
+REFERENCE_SEED = 7
+# FLOP per interaction in the reference's GFLOPS figure (src/nbody.cu:1027).
+FLOPS_PER_INTERACTION = 20
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _f32p(a: np.ndarray):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _f64p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _dev(t) -> int:
+    """Device address of a CUDA tensor (or an int address)."""
+    if isinstance(t, int):
+        return t
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA tensor")
+    return t.data_ptr()
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        return _torch().cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+# ---------------------------------------------------------------------------
+# Drop-in algorithm row
+# ---------------------------------------------------------------------------
+def ComputeGravitation_GPU_GB300(force, posMass, softeningSquared: float, N: int) -> float:
+    """The reference's AOS algorithm signature: device buffers in, elapsed
+    milliseconds out (0.0 means failure / skip, src/nbody.cu:385-386)."""
+    return float(load().ComputeGravitation_GPU_GB300(_dev(force), _dev(posMass),
+                                                     softeningSquared, N))
+
+
+def release_workspace() -> None:
+    load().nbgb_release_workspace()
+
+
+# ---------------------------------------------------------------------------
+# Stream-ordered force
+# ---------------------------------------------------------------------------
+def force_plan(N: int, config: int = -1, nsplit: int = -1):
+    c, s, w = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+    check(load().nbgb_force_plan(N, config, nsplit, ctypes.byref(c), ctypes.byref(s),
+                                 ctypes.byref(w)), "nbgb_force_plan")
+    return c.value, s.value, w.value
+
+
+def force_config_names():
+    lib = load()
+    return [lib.nbgb_force_config_name(i).decode() for i in range(lib.nbgb_force_num_configs())]
+
+
+class Workspace:
+    """Device scratch for force(); grows on demand (a torch byte tensor)."""
+
+    def __init__(self):
+        self.buf = None
+
+    def get(self, nbytes: int):
+        torch = _torch()
+        if self.buf is None or self.buf.numel() < nbytes:
+            self.buf = torch.empty(max(nbytes, 256), dtype=torch.uint8, device="cuda")
+        return self.buf
+
+
+_default_ws = Workspace()
+
+
+def force(posMass, softeningSquared: float, out=None, stream=None, workspace: Workspace = None,
+          config: int = -1, nsplit: int = -1):
+    """F_i = sum_j m_j d_ij / (|d_ij|^2 + eps2)^1.5 for a (N,4) float32 CUDA
+    tensor {x,y,z,m}; returns (N,4) {fx,fy,fz,0}."""
+    torch = _torch()
+    n = posMass.shape[0]
+    if out is None:
+        out = torch.empty((n, 4), dtype=torch.float32, device=posMass.device)
+    if n == 0:
+        return out
+    _, _, wsb = force_plan(n, config, nsplit)
+    ws = (workspace or _default_ws).get(wsb)
+    check(load().nbgb_force_ex(_dev(out), _dev(posMass), softeningSquared, n, ws.data_ptr(),
+                               ws.numel(), config, nsplit, _stream(stream)), "nbgb_force")
+    return out
+
+
+def integrate_reference(posMass, velInvMass, force_, dt: float, damping: float, stream=None):
+    """In place on (N,4) float32 CUDA tensors (src/nbody.cu:158-182)."""
+    n = posMass.shape[0]
+    check(load().nbgb_integrate_reference(_dev(posMass), _dev(velInvMass), _dev(force_), dt,
+                                          damping, n, _stream(stream)),
+          "nbgb_integrate_reference")
+
+
+def measure_peak(which: str, iters: int = 4096, reps: int = 5):
+    """Measured pipe throughput: 'ffma' / 'ffma2' (FLOP/s) or 'mufu' (rsqrt/s)."""
+    code = {"ffma": 0, "ffma2": 1, "mufu": 2}[which]
+    rate, ms = ctypes.c_double(), ctypes.c_float()
+    check(load().nbgb_measure_peak(code, iters, reps, ctypes.byref(rate), ctypes.byref(ms)),
+          "nbgb_measure_peak")
+    return rate.value, ms.value
+
+
+def last_status() -> int:
+    return int(load().nbgb_last_status())
+
+
+# ---------------------------------------------------------------------------
+# Device-resident simulation
+# ---------------------------------------------------------------------------
+class System:
+    """State resident in HBM; step() = force + integrate per step (one CUDA
+    graph per step body), no host round trip."""
+
+    def __init__(self, N: int, integrator: int = INTEGRATOR_REFERENCE,
+                 softeningSquared: float = 1e-4, dt: float = 0.01, damping: float = 1.0):
+        self.lib = load()
+        self.n = N
+        self.integrator = integrator
+        self.h = self.lib.nbgb_system_create(N, integrator, softeningSquared, dt, damping)
+        if not self.h:
+            raise NbgbError(-6, "nbgb_system_create")
+
+    def close(self):
+        if self.h:
+            self.lib.nbgb_system_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, posMass: np.ndarray, velInvMass: np.ndarray):
+        pm = np.ascontiguousarray(posMass, np.float32)
+        vm = np.ascontiguousarray(velInvMass, np.float32)
+        assert pm.shape == (self.n, 4) and vm.shape == (self.n, 4)
+        check(self.lib.nbgb_system_set_state(self.h, _f32p(pm), _f32p(vm)), "set_state")
+
+    def set_state64(self, pos3: np.ndarray, vel3: np.ndarray, mass: np.ndarray):
+        p = np.ascontiguousarray(pos3, np.float64)
+        v = np.ascontiguousarray(vel3, np.float64)
+        m = np.ascontiguousarray(mass, np.float32)
+        check(self.lib.nbgb_system_set_state64(self.h, _f64p(p), _f64p(v), _f32p(m)),
+              "set_state64")
+
+    def step(self, nsteps: int = 1):
+        check(self.lib.nbgb_system_step(self.h, nsteps), "step")
+
+    def use_graph(self, enable: bool):
+        check(self.lib.nbgb_system_set_graph(self.h, int(enable)), "set_graph")
+
+    def synchronize(self):
+        check(self.lib.nbgb_system_synchronize(self.h), "synchronize")
+
+    def set_timing(self, enable: bool):
+        check(self.lib.nbgb_system_set_timing(self.h, int(enable)), "set_timing")
+
+    def last_force_ms(self) -> float:
+        ms = ctypes.c_float()
+        check(self.lib.nbgb_system_last_force_ms(self.h, ctypes.byref(ms)), "last_force_ms")
+        return ms.value
+
+    def get_state(self):
+        pm = np.zeros((self.n, 4), np.float32)
+        vm = np.zeros((self.n, 4), np.float32)
+        check(self.lib.nbgb_system_get_state(self.h, _f32p(pm), _f32p(vm)), "get_state")
+        return pm, vm
+
+    def get_state64(self):
+        p = np.zeros((self.n, 3), np.float64)
+        v = np.zeros((self.n, 3), np.float64)
+        check(self.lib.nbgb_system_get_state64(self.h, _f64p(p), _f64p(v)), "get_state64")
+        return p, v
+
+    def get_force(self) -> np.ndarray:
+        f = np.zeros((self.n, 4), np.float32)
+        check(self.lib.nbgb_system_get_force(self.h, _f32p(f)), "get_force")
+        return f
+
+    def plan(self):
+        c, s = ctypes.c_int(), ctypes.c_int()
+        check(self.lib.nbgb_system_plan(self.h, ctypes.byref(c), ctypes.byref(s)), "plan")
+        return c.value, s.value
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.nbgb_system_stream(self.h) or 0)
+
+
+# ---------------------------------------------------------------------------
+# Initial conditions, metrics (host)
+# ---------------------------------------------------------------------------
+def ic_reference(N: int, seed: int = REFERENCE_SEED, scale: float = REFERENCE_SCALE,
+                 velscale: float = REFERENCE_VELOCITY_SCALE):
+    """The reference driver's bodies (src/nbody_util.cpp:102-144)."""
+    pm = np.zeros((N, 4), np.float32)
+    vm = np.zeros((N, 4), np.float32)
+    check(load().nbgb_ic_reference(_f32p(pm), _f32p(vm), N, scale, velscale, seed),
+          "ic_reference")
+    return pm, vm
+
+
+def ic_uniform_ball(N: int, seed: int, radius: float = 1.0, m_lo: float = 1.0,
+                    m_hi: float = 1.0):
+    """Uniform ball; mass U[m_lo, m_hi]/N (equal 1/N by default); v = 0."""
+    pm = np.zeros((N, 4), np.float32)
+    vm = np.zeros((N, 4), np.float32)
+    check(load().nbgb_ic_uniform_ball(_f32p(pm), _f32p(vm), N, radius, m_lo, m_hi, seed),
+          "ic_uniform_ball")
+    return pm, vm
+
+
+def ic_plummer(N: int, seed: int):
+    """Plummer sphere (G=M=a=1): (pos3 f64, vel3 f64, posMass f32, velInvMass f32)."""
+    p = np.zeros((N, 3), np.float64)
+    v = np.zeros((N, 3), np.float64)
+    pm = np.zeros((N, 4), np.float32)
+    vm = np.zeros((N, 4), np.float32)
+    check(load().nbgb_ic_plummer(_f64p(p), _f64p(v), _f32p(pm), _f32p(vm), N, seed),
+          "ic_plummer")
+    return p, v, pm, vm
+
+
+def crosscheck_max_rel_error(force_: np.ndarray, golden: np.ndarray) -> float:
+    f = np.ascontiguousarray(force_, np.float32)
+    g = np.ascontiguousarray(golden, np.float32)
+    return float(load().nbgb_crosscheck_max_rel_error(_f32p(f), _f32p(g), f.shape[0]))
+
+
+def force_error_stats(force_: np.ndarray, truth3: np.ndarray, idx=None):
+    """(max, rms) of per-body |F - T| / |T| against FP64 truth rows."""
+    f = np.ascontiguousarray(force_, np.float32)
+    t = np.ascontiguousarray(truth3, np.float64)
+    mx, rms = ctypes.c_double(), ctypes.c_double()
+    ip = None
+    if idx is not None:
+        idx = np.ascontiguousarray(idx, np.int64)
+        ip = idx.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))
+    check(load().nbgb_force_error_stats(_f32p(f), _f64p(t), ip, t.shape[0], ctypes.byref(mx),
+                                        ctypes.byref(rms)), "force_error_stats")
+    return mx.value, rms.value
+
+
+def interactions_per_second(N: int, ms: float) -> float:
+    """src/nbody.cu:1026: N^2 interactions (self pairs included) per ms."""
+    return float(N) * float(N) * 1000.0 / ms
+
+
+def reference_line(name: str, N: int, ms: float, rel_error=None, name_width: int = 0) -> str:
+    """The reference's per-step stdout line (src/nbody.cu:1024-1053)."""
+    ips = interactions_per_second(N, ms)
+    gflops = ips * FLOPS_PER_INTERACTION * 1e-9
+    if ips > 1e9:
+        s = f"{name:>{name_width}}: {ms:8.2f} ms = {ips / 1e9:8.3f}x10^9 interactions/s ({gflops:9.2f} GFLOPS)"
+    else:
+        s = f"{name:>{name_width}}: {ms:8.2f} ms = {ips / 1e6:8.3f}x10^6 interactions/s ({gflops:9.2f} GFLOPS)"
+    if rel_error is not None:
+        s += f" (Rel. error: {rel_error:E})"
+    return s

@@ -1,0 +1,642 @@
+// force.cu -- all-pairs softened gravity on GB300 (sm_103a).
+//
+// Computes, for every target body i,
+//     F_i = sum_j m_j (p_j - p_i) / (|p_j - p_i|^2 + eps2)^(3/2)
+// exactly the sum of src/bodybodyInteraction.cuh:40-65 over all j (self term
+// included; it is 0 because eps2 > 0), as the reference's
+// ComputeGravitation_* algorithms do (e.g. src/nbody_GPU_Shared.cu:42-81).
+//
+// Structure (one launch per force evaluation, after a tiny pack launch):
+//
+//   pack_jstream   float4 AOS {x,y,z,m} -> "j-stream": bodies in pairs laid
+//                  out {x0,x1,y0,y1,z0,z1,m0,m1} (32 B per pair), padded with
+//                  zero-mass bodies to a whole number of j-tiles.  The same
+//                  launch zeroes the split counters.
+//   force_kernel   one CTA per work unit (i-block, j-split).  The i-block is
+//                  W warps x 32 lanes x K target bodies held in registers.  The
+//                  j-split's tiles of JT bodies are streamed into shared memory
+//                  by 1-D bulk copies (cp.async.bulk, TMA) into a STAGES-deep
+//                  ring completing on mbarriers, read back with broadcast
+//                  128-bit shared loads, and evaluated two interactions per
+//                  instruction with the f32x2 FP32 instructions (rsqrt on the
+//                  MUFU pipe).  Each tile's FP32 partial sum is folded into a
+//                  per-body compensated (TwoSum) running sum.
+//                  With nsplit > 1 the j-range of an i-block is cut into
+//                  nsplit slices so that the number of units fills the GPU's
+//                  SMs evenly.  Each unit writes its (hi, lo) partials; the
+//                  last unit of an i-block to finish (atomic counter) adds the
+//                  partials of slices 0..nsplit-1 in fixed order, so the result
+//                  does not depend on which unit finishes last.
+//
+// The drop-in entry point ComputeGravitation_GPU_GB300 has the reference's
+// pfnComputeGravitation_AOS_t signature (src/nbody.h:68) and its conventions
+// (device pointers, legacy stream, event-timed milliseconds returned, 0 on
+// error, synchronised before return: src/nbody_GPU_Shared.cu:83-103).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "nbgb_device.cuh"
+#include "nbgb_internal.h"
+#include "nbody_gb300.h"
+
+namespace nbgb {
+
+struct ForceParams {
+    const float4 *__restrict__ ipos;     // targets, AOS {x,y,z,m}
+    const float4 *__restrict__ jstream;  // sources, paired layout, ntiles*JT bodies
+    float4 *__restrict__ force;          // output {fx,fy,fz,0}
+    float4 *__restrict__ part_hi;        // [nsplit][ni_pad] (nsplit > 1 only)
+    float4 *__restrict__ part_lo;        // [nsplit][ni_pad]
+    unsigned *__restrict__ counters;     // [nblocks]
+    int n;
+    int ntiles;
+    int nsplit;
+    int ni_pad;
+    float eps2;
+};
+
+// ---------------------------------------------------------------------------
+// pack: AOS -> paired j-stream, zero-mass padding, counter reset.
+// ---------------------------------------------------------------------------
+__global__ void pack_jstream_kernel(const float4 *__restrict__ pm, float4 *__restrict__ js, int n,
+                                    int npad, unsigned *__restrict__ counters, int ncounters) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // pair index
+    if (q < ncounters)
+        counters[q] = 0u;
+    if (2 * q >= npad)
+        return;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 b0 = (2 * q < n) ? pm[2 * q] : z;
+    float4 b1 = (2 * q + 1 < n) ? pm[2 * q + 1] : z;
+    js[2 * q] = make_float4(b0.x, b1.x, b0.y, b1.y);
+    js[2 * q + 1] = make_float4(b0.z, b1.z, b0.w, b1.w);
+}
+
+// ---------------------------------------------------------------------------
+// force kernel
+// ---------------------------------------------------------------------------
+template <int W, int K, int JT, int STAGES, bool PACKED, int UNROLL, int MINB>
+__global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
+    constexpr int NT = W * 32;
+    constexpr int BI = NT * K;
+    constexpr uint32_t TILE_BYTES = JT * 16u;
+    static_assert(JT % 2 == 0, "tiles hold whole pairs");
+
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float4 *ring = reinterpret_cast<float4 *>(smem_raw);
+    __shared__ __align__(8) uint64_t full[STAGES];
+    __shared__ int s_last;
+
+    const int tid = threadIdx.x;
+    const int unit = blockIdx.x;
+    const int ib = unit / p.nsplit;
+    const int r = unit - ib * p.nsplit;
+    const int t_begin = (int)(((long long)r * p.ntiles) / p.nsplit);
+    const int t_end = (int)(((long long)(r + 1) * p.ntiles) / p.nsplit);
+    const int nt = t_end - t_begin;
+
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; s++)
+            mbar_init(&full[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int issued = 0;  // tiles whose copy has been issued (meaningful in thread 0)
+    if (tid == 0) {
+        for (int s = 0; s < STAGES && s < nt; s++) {
+            mbar_expect_tx(&full[s], TILE_BYTES);
+            bulk_g2s(ring + s * JT, p.jstream + (size_t)(t_begin + s) * JT, TILE_BYTES, &full[s]);
+            issued++;
+        }
+    }
+
+    // Targets: thread tid owns bodies ib*BI + k*NT + tid (coalesced loads).
+    f2 nx[K], ny[K], nz[K];     // packed mode: (-x,-x) etc.
+    float px[K], py[K], pz[K];  // scalar mode
+    float hx[K], hy[K], hz[K], lx[K], ly[K], lz[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int i = ib * BI + k * NT + tid;
+        float4 b = (i < p.n) ? p.ipos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        px[k] = b.x;
+        py[k] = b.y;
+        pz[k] = b.z;
+        nx[k] = f2_pack(-b.x, -b.x);
+        ny[k] = f2_pack(-b.y, -b.y);
+        nz[k] = f2_pack(-b.z, -b.z);
+        hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
+    }
+    const f2 eps2p = f2_pack(p.eps2, p.eps2);
+    const f2 zero2 = f2_pack(0.f, 0.f);
+
+    bool failed = false;
+    int t = 0;
+    for (; t < nt; t++) {
+        const int s = t % STAGES;
+        const uint32_t parity = (uint32_t)((t / STAGES) & 1);
+        const bool ok = mbar_wait_bounded(&full[s], parity);
+        if (ok) {
+            const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(ring + s * JT);
+            if (PACKED) {
+                f2 ax[K], ay[K], az[K];
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    ax[k] = ay[k] = az[k] = zero2;
+#pragma unroll UNROLL
+                for (int q = 0; q < JT / 2; q++) {
+                    const ulonglong2 a = tp[2 * q];
+                    const ulonglong2 b = tp[2 * q + 1];
+#pragma unroll
+                    for (int k = 0; k < K; k++)
+                        pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p, ax[k],
+                                       ay[k], az[k]);
+                }
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    float l, h;
+                    f2_unpack(ax[k], l, h);
+                    comp_add(hx[k], lx[k], l + h);
+                    f2_unpack(ay[k], l, h);
+                    comp_add(hy[k], ly[k], l + h);
+                    f2_unpack(az[k], l, h);
+                    comp_add(hz[k], lz[k], l + h);
+                }
+            } else {
+                float ax[K], ay[K], az[K];
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    ax[k] = ay[k] = az[k] = 0.f;
+                const float4 *tf = reinterpret_cast<const float4 *>(tp);
+#pragma unroll UNROLL
+                for (int q = 0; q < JT / 2; q++) {
+                    const float4 a = tf[2 * q];      // x0 x1 y0 y1
+                    const float4 b = tf[2 * q + 1];  // z0 z1 m0 m1
+#pragma unroll
+                    for (int k = 0; k < K; k++) {
+                        pair_interact1(a.x, a.z, b.x, b.z, px[k], py[k], pz[k], p.eps2, ax[k],
+                                       ay[k], az[k]);
+                        pair_interact1(a.y, a.w, b.y, b.w, px[k], py[k], pz[k], p.eps2, ax[k],
+                                       ay[k], az[k]);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    comp_add(hx[k], lx[k], ax[k]);
+                    comp_add(hy[k], ly[k], ay[k]);
+                    comp_add(hz[k], lz[k], az[k]);
+                }
+            }
+        }
+        // Every thread reaches this barrier (the waits are bounded), so a
+        // timeout anywhere makes the whole CTA leave together.
+        failed = __syncthreads_or(!ok) != 0;
+        if (failed)
+            break;
+        if (tid == 0 && t + STAGES < nt) {
+            mbar_expect_tx(&full[s], TILE_BYTES);
+            bulk_g2s(ring + s * JT, p.jstream + (size_t)(t_begin + t + STAGES) * JT, TILE_BYTES,
+                     &full[s]);
+            issued++;
+        }
+    }
+    if (failed) {
+        // Let copies still in flight (tiles t .. issued-1) land before the
+        // CTA's shared memory is released, again with a bounded wait, then
+        // leave without writing results.
+        if (tid == 0)
+            for (int u = t; u < issued; u++)
+                (void)mbar_wait_bounded(&full[u % STAGES], (uint32_t)((u / STAGES) & 1),
+                                        100000000ull);
+        return;
+    }
+
+    if (p.nsplit == 1) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const int i = ib * BI + k * NT + tid;
+            if (i < p.n)
+                p.force[i] = make_float4(hx[k] + lx[k], hy[k] + ly[k], hz[k] + lz[k], 0.f);
+        }
+        return;
+    }
+
+    // Split j-range: publish partials, the last unit of the i-block combines.
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const size_t o = (size_t)r * p.ni_pad + (size_t)(ib * BI + k * NT + tid);
+        p.part_hi[o] = make_float4(hx[k], hy[k], hz[k], 0.f);
+        p.part_lo[o] = make_float4(lx[k], ly[k], lz[k], 0.f);
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned prev = atomicAdd(&p.counters[ib], 1u);
+        s_last = (prev == (unsigned)(p.nsplit - 1));
+        if (s_last)
+            p.counters[ib] = 0u;  // ready for the next launch
+    }
+    __syncthreads();
+    if (!s_last)
+        return;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int i = ib * BI + k * NT + tid;
+        if (i >= p.n)
+            continue;
+        float Hx = 0.f, Hy = 0.f, Hz = 0.f, Lx = 0.f, Ly = 0.f, Lz = 0.f;
+        for (int rr = 0; rr < p.nsplit; rr++) {
+            float4 h, l;
+            if (rr == r) {
+                h = make_float4(hx[k], hy[k], hz[k], 0.f);
+                l = make_float4(lx[k], ly[k], lz[k], 0.f);
+            } else {
+                const size_t o = (size_t)rr * p.ni_pad + (size_t)i;
+                h = __ldcg(p.part_hi + o);
+                l = __ldcg(p.part_lo + o);
+            }
+            comp_add(Hx, Lx, h.x);
+            comp_add(Hy, Ly, h.y);
+            comp_add(Hz, Lz, h.z);
+            Lx += l.x;
+            Ly += l.y;
+            Lz += l.z;
+        }
+        p.force[i] = make_float4(Hx + Lx, Hy + Ly, Hz + Lz, 0.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Configurations.  The planner picks one per N (or a caller forces one).
+// ---------------------------------------------------------------------------
+struct ForceConfig {
+    int warps, k, jt, stages;
+    bool packed;
+    const void *fn;
+    const char *name;
+};
+
+// W warps, K targets per thread, JT sources per tile, ST ring stages, packed
+// f32x2 or scalar, inner unroll, minimum resident CTAs (register cap).
+#define NBGB_CFG(W, K, JT, ST, PK, UN, MB, PIPE)                                           \
+    {W, K, JT, ST, PK, (const void *)force_kernel<W, K, JT, ST, PK, UN, MB>,               \
+     "w" #W "_k" #K "_jt" #JT "_s" #ST "_" PIPE}
+
+static const ForceConfig kConfigs[] = {
+    NBGB_CFG(8, 4, 512, 3, true, 4, 2, "f32x2"),  // 0: BI 1024
+    NBGB_CFG(4, 4, 512, 3, true, 4, 4, "f32x2"),  // 1: BI 512
+    NBGB_CFG(8, 2, 256, 4, true, 8, 2, "f32x2"),  // 2: BI 512
+    NBGB_CFG(4, 2, 256, 4, true, 8, 4, "f32x2"),  // 3: BI 256
+    NBGB_CFG(8, 4, 512, 3, false, 4, 2, "f32"),   // 4: scalar FP32 pipe, BI 1024
+    NBGB_CFG(4, 8, 512, 3, true, 2, 2, "f32x2"),  // 5: BI 1024, 8 targets per thread
+};
+static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
+static const int kDefaultCandidates[] = {0, 1, 2, 3, 5};
+
+static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct DeviceInfo {
+    int sms = 0;
+    int occ[16] = {0};
+    bool ok = false;
+};
+
+static std::mutex g_dev_mu;
+static DeviceInfo g_dev[64];
+
+static const DeviceInfo *device_info() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return nullptr;
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    DeviceInfo &d = g_dev[dev];
+    if (d.ok)
+        return &d;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
+        return nullptr;
+    d.sms = prop.multiProcessorCount;
+    for (int c = 0; c < kNumConfigs; c++) {
+        const ForceConfig &cf = kConfigs[c];
+        const size_t smem = (size_t)cf.stages * cf.jt * 16;
+        if (cudaFuncSetAttribute(cf.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return nullptr;
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cf.fn, cf.warps * 32, smem) !=
+            cudaSuccess)
+            return nullptr;
+        d.occ[c] = occ;
+    }
+    d.ok = true;
+    return &d;
+}
+
+static void fill_layout(ForcePlan &pl, size_t n) {
+    const ForceConfig &cf = kConfigs[pl.config];
+    const size_t bi = (size_t)cf.warps * 32 * cf.k;
+    pl.n = n;
+    pl.block_bodies = (int)bi;
+    pl.tile_bodies = cf.jt;
+    pl.nblocks = (int)((n + bi - 1) / bi);
+    pl.ntiles = (int)((n + cf.jt - 1) / cf.jt);
+    pl.ni_pad = (size_t)pl.nblocks * bi;
+    pl.off_js = 0;
+    size_t o = align_up((size_t)pl.ntiles * cf.jt * 16, 256);
+    if (pl.nsplit > 1) {
+        pl.off_hi = o;
+        o = align_up(o + (size_t)pl.nsplit * pl.ni_pad * 16, 256);
+        pl.off_lo = o;
+        o = align_up(o + (size_t)pl.nsplit * pl.ni_pad * 16, 256);
+        pl.off_cnt = o;
+        o = align_up(o + (size_t)pl.nblocks * 4, 256);
+    } else {
+        pl.off_hi = pl.off_lo = pl.off_cnt = 0;
+    }
+    pl.workspace_bytes = o;
+}
+
+// Cost model: units run in waves of (SMs x resident CTAs); a unit's time is
+// proportional to tiles x JT x BI x (resident CTAs per SM), i.e. the SM's
+// interaction throughput is assumed equal across configurations.  The chosen
+// plan minimises waves x per-unit time.
+int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
+    if (n == 0 || n > kMaxBodies)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const DeviceInfo *d = device_info();
+    if (!d)
+        return NBGB_ERR_CUDA;
+    std::vector<int> cands;
+    if (force_config >= 0) {
+        if (force_config >= kNumConfigs)
+            return NBGB_ERR_INVALID_ARGUMENT;
+        cands.push_back(force_config);
+    } else {
+        for (int c : kDefaultCandidates)
+            cands.push_back(c);
+    }
+    double best = 1e300;
+    int best_c = -1, best_s = 1;
+    for (int c : cands) {
+        const ForceConfig &cf = kConfigs[c];
+        const int occ = d->occ[c];
+        if (occ <= 0)
+            continue;
+        const double slots = (double)d->sms * occ;
+        const long long bi = (long long)cf.warps * 32 * cf.k;
+        const long long nb = ((long long)n + bi - 1) / bi;
+        const long long ntl = ((long long)n + cf.jt - 1) / cf.jt;
+        int s_lo = 1, s_hi = (int)std::min<long long>(ntl, 256);
+        if (force_nsplit > 0)
+            s_lo = s_hi = (int)std::min<long long>(force_nsplit, ntl);
+        for (int s = s_lo; s <= s_hi; s++) {
+            const long long units = nb * s;
+            if (units > (1ll << 31) - 1)
+                continue;
+            const double waves = std::ceil((double)units / slots);
+            const double tiles = std::ceil((double)ntl / s);
+            // + small per-unit overhead (prologue, partial write and combine)
+            const double t = waves * (tiles * cf.jt + 64.0 + (s > 1 ? 32.0 * s : 0.0)) *
+                             (double)bi * occ;
+            if (t < best * (1.0 - 1e-9)) {
+                best = t;
+                best_c = c;
+                best_s = s;
+            }
+        }
+    }
+    if (best_c < 0)
+        return NBGB_ERR_UNSUPPORTED;
+    pl.config = best_c;
+    pl.nsplit = best_s;
+    fill_layout(pl, n);
+    return NBGB_OK;
+}
+
+int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,
+                 float eps2, void *workspace, cudaStream_t stream) {
+    const ForceConfig &cf = kConfigs[pl.config];
+    char *ws = (char *)workspace;
+    ForceParams p;
+    p.ipos = posMass;
+    p.jstream = jstream ? jstream : (const float4 *)(ws + pl.off_js);
+    p.force = force;
+    p.part_hi = pl.nsplit > 1 ? (float4 *)(ws + pl.off_hi) : nullptr;
+    p.part_lo = pl.nsplit > 1 ? (float4 *)(ws + pl.off_lo) : nullptr;
+    p.counters = pl.nsplit > 1 ? (unsigned *)(ws + pl.off_cnt) : nullptr;
+    p.n = (int)pl.n;
+    p.ntiles = pl.ntiles;
+    p.nsplit = pl.nsplit;
+    p.ni_pad = (int)pl.ni_pad;
+    p.eps2 = eps2;
+    const size_t smem = (size_t)cf.stages * cf.jt * 16;
+    void *args[] = {&p};
+    const unsigned grid = (unsigned)((long long)pl.nblocks * pl.nsplit);
+    cudaError_t e = cudaLaunchKernel(cf.fn, dim3(grid), dim3(cf.warps * 32), args, smem, stream);
+    return e == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
+}
+
+int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream) {
+    char *ws = (char *)workspace;
+    float4 *js = (float4 *)(ws + pl.off_js);
+    unsigned *cnt = pl.nsplit > 1 ? (unsigned *)(ws + pl.off_cnt) : nullptr;
+    const int npad = pl.ntiles * pl.tile_bodies;
+    const int ncnt = pl.nsplit > 1 ? pl.nblocks : 0;
+    const int work = std::max(npad / 2, ncnt);
+    const int tb = 256;
+    pack_jstream_kernel<<<(work + tb - 1) / tb, tb, 0, stream>>>(posMass, js, (int)pl.n, npad, cnt,
+                                                                  ncnt);
+    return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
+}
+
+const char *config_name(int c) { return (c >= 0 && c < kNumConfigs) ? kConfigs[c].name : "?"; }
+int num_configs() { return kNumConfigs; }
+
+static NBGB_STATUS_READER(read_status_force)
+
+int read_and_clear_status(unsigned *bits) {
+    *bits = 0;
+    int rc = read_status_force(bits);
+    return rc;
+}
+
+// Workspace cache for the drop-in entry point (one per device, grow-only).
+struct WsCache {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+static std::mutex g_ws_mu;
+static WsCache g_ws[64];
+
+static void *cached_workspace(size_t bytes) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return nullptr;
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    WsCache &w = g_ws[dev];
+    if (w.bytes >= bytes && w.ptr)
+        return w.ptr;
+    if (w.ptr) {
+        cudaFree(w.ptr);
+        w.ptr = nullptr;
+        w.bytes = 0;
+    }
+    if (cudaMalloc(&w.ptr, bytes) != cudaSuccess) {
+        w.ptr = nullptr;
+        return nullptr;
+    }
+    w.bytes = bytes;
+    return w.ptr;
+}
+
+void release_workspaces() {
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    int cur = 0;
+    cudaGetDevice(&cur);
+    for (int d = 0; d < 64; d++) {
+        if (g_ws[d].ptr) {
+            cudaSetDevice(d);
+            cudaFree(g_ws[d].ptr);
+            g_ws[d].ptr = nullptr;
+            g_ws[d].bytes = 0;
+        }
+    }
+    cudaSetDevice(cur);
+}
+
+}  // namespace nbgb
+
+using namespace nbgb;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+NBGB_API size_t nbgb_force_workspace_bytes(size_t N) {
+    ForcePlan pl;
+    if (plan_force(N, -1, -1, pl) != NBGB_OK)
+        return 0;
+    return pl.workspace_bytes;
+}
+
+NBGB_API int nbgb_force_plan(size_t N, int config, int nsplit, int *out_config, int *out_nsplit,
+                             size_t *out_workspace_bytes) {
+    ForcePlan pl;
+    int rc = plan_force(N, config, nsplit, pl);
+    if (rc != NBGB_OK)
+        return rc;
+    if (out_config)
+        *out_config = pl.config;
+    if (out_nsplit)
+        *out_nsplit = pl.nsplit;
+    if (out_workspace_bytes)
+        *out_workspace_bytes = pl.workspace_bytes;
+    return NBGB_OK;
+}
+
+NBGB_API const char *nbgb_force_config_name(int config) { return config_name(config); }
+NBGB_API int nbgb_force_num_configs(void) { return num_configs(); }
+
+NBGB_API int nbgb_force_ex(float *force, const float *posMass, float softeningSquared, size_t N,
+                           void *workspace, size_t workspace_bytes, int config, int nsplit,
+                           void *stream) {
+    if (N == 0)
+        return NBGB_OK;
+    if (!force || !posMass)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (((uintptr_t)force | (uintptr_t)posMass) & 15u)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    ForcePlan pl;
+    int rc = plan_force(N, config, nsplit, pl);
+    if (rc != NBGB_OK)
+        return rc;
+    if (!workspace || workspace_bytes < pl.workspace_bytes || ((uintptr_t)workspace & 255u))
+        return NBGB_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = launch_pack(pl, (const float4 *)posMass, workspace, st);
+    if (rc != NBGB_OK)
+        return rc;
+    return launch_force(pl, (float4 *)force, (const float4 *)posMass, nullptr, softeningSquared,
+                        workspace, st);
+}
+
+NBGB_API int nbgb_force(float *force, const float *posMass, float softeningSquared, size_t N,
+                        void *workspace, size_t workspace_bytes, void *stream) {
+    return nbgb_force_ex(force, posMass, softeningSquared, N, workspace, workspace_bytes, -1, -1,
+                         stream);
+}
+
+NBGB_API float ComputeGravitation_GPU_GB300(float *force, float *posMass, float softeningSquared,
+                                            size_t N) {
+    float ms = 0.0f;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ForcePlan pl;
+    void *ws = nullptr;
+    if (N == 0 || !force || !posMass)
+        return 0.0f;
+    if (plan_force(N, -1, -1, pl) != NBGB_OK)
+        return 0.0f;
+    ws = cached_workspace(pl.workspace_bytes);
+    if (!ws)
+        return 0.0f;
+    if (cudaEventCreate(&ev0) != cudaSuccess || cudaEventCreate(&ev1) != cudaSuccess)
+        goto done;
+    if (cudaEventRecord(ev0, nullptr) != cudaSuccess)
+        goto done;
+    if (launch_pack(pl, (const float4 *)posMass, ws, nullptr) != NBGB_OK)
+        goto done;
+    if (launch_force(pl, (float4 *)force, (const float4 *)posMass, nullptr, softeningSquared, ws,
+                     nullptr) != NBGB_OK)
+        goto done;
+    if (cudaEventRecord(ev1, nullptr) != cudaSuccess)
+        goto done;
+    if (cudaDeviceSynchronize() != cudaSuccess)
+        goto done;
+    {
+        unsigned bits = 0;
+        if (read_and_clear_status(&bits) != NBGB_OK || bits != 0)
+            goto done;
+    }
+    if (cudaEventElapsedTime(&ms, ev0, ev1) != cudaSuccess)
+        ms = 0.0f;
+done:
+    if (ev1)
+        cudaEventDestroy(ev1);
+    if (ev0)
+        cudaEventDestroy(ev0);
+    return ms;
+}
+
+NBGB_API void nbgb_release_workspace(void) { release_workspaces(); }
+
+NBGB_API int nbgb_last_status(void) {
+    unsigned bits = 0;
+    int rc = read_and_clear_status(&bits);
+    return rc != NBGB_OK ? rc : (int)bits;
+}
+
+NBGB_API const char *nbgb_status_string(int code) {
+    switch (code) {
+    case NBGB_OK: return "ok";
+    case NBGB_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case NBGB_ERR_WORKSPACE: return "workspace missing, misaligned or too small";
+    case NBGB_ERR_CUDA: return "CUDA runtime error";
+    case NBGB_ERR_DEVICE: return "a kernel reported a device status (bounded wait ran out)";
+    case NBGB_ERR_UNSUPPORTED: return "unsupported device or configuration";
+    case NBGB_ERR_NO_MEMORY: return "out of memory or over the memory budget";
+    case NBGB_ERR_TOO_LARGE: return "size exceeds the documented maximum";
+    default: return "unknown status";
+    }
+}
+
+NBGB_API const char *nbgb_version(void) { return "nbody_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,203 @@
+// nbgb_device.cuh -- device-side building blocks shared by the GB300 kernels.
+//
+//  * the pair interaction of src/bodybodyInteraction.cuh:40-65, in a scalar
+//    form and in a packed form that evaluates two interactions per
+//    instruction with the sm_100-family f32x2 FP32 instructions;
+//  * Knuth's TwoSum for compensated accumulation across j-tiles;
+//  * mbarrier + 1-D bulk-copy (TMA) wrappers whose waits are bounded in time:
+//    a wait that runs out sets a bit in the device status word and returns
+//    false instead of spinning forever.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "nbgb_status.h"
+
+namespace nbgb {
+
+// Device status word: bits from nbgb_status.h, OR-ed in by kernels that hit a
+// bounded wait or an internal consistency check.  Each translation unit has
+// its own copy (no relocatable device code); NBGB_STATUS_READER defines the
+// host function that reads and clears it, and nbgb_last_status() ORs them.
+static __device__ unsigned int g_status = 0;
+
+#define NBGB_STATUS_READER(name)                                                   \
+    int name(unsigned *bits) {                                                     \
+        unsigned v = 0, z = 0;                                                     \
+        if (cudaMemcpyFromSymbol(&v, g_status, sizeof(v)) != cudaSuccess)          \
+            return NBGB_ERR_CUDA;                                                  \
+        if (v && cudaMemcpyToSymbol(g_status, &z, sizeof(z)) != cudaSuccess)       \
+            return NBGB_ERR_CUDA;                                                  \
+        *bits |= v;                                                                \
+        return NBGB_OK;                                                            \
+    }
+
+// ---------------------------------------------------------------------------
+// Packed FP32 pairs.  A u64 holds (lo, hi) = two binary32 values in adjacent
+// registers; add/fma/mul.f32x2 run both halves in one instruction.
+// ---------------------------------------------------------------------------
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 f2_pack(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// MUFU reciprocal square root (the reference's rsqrtf on the SFU pipe).
+__device__ __forceinline__ float rsqrt_mufu(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Two interactions at once: sources (x0,x1),(y0,y1),(z0,z1),(m0,m1) against
+// one target whose negated position is held duplicated in (nx,nx) etc.
+// Same arithmetic as bodyBodyInteraction, with eps2 folded into the first FMA
+// of the squared distance.
+__device__ __forceinline__ void pair_interact2(f2 sx, f2 sy, f2 sz, f2 sm,
+                                               f2 nx, f2 ny, f2 nz, f2 eps2,
+                                               f2 &ax, f2 &ay, f2 &az) {
+    f2 dx = f2_add(sx, nx);
+    f2 dy = f2_add(sy, ny);
+    f2 dz = f2_add(sz, nz);
+    f2 d2 = f2_fma(dx, dx, eps2);
+    d2 = f2_fma(dy, dy, d2);
+    d2 = f2_fma(dz, dz, d2);
+    float d2l, d2h;
+    f2_unpack(d2, d2l, d2h);
+    f2 inv = f2_pack(rsqrt_mufu(d2l), rsqrt_mufu(d2h));
+    f2 inv2 = f2_mul(inv, inv);
+    f2 s = f2_mul(sm, inv);
+    s = f2_mul(s, inv2);
+    ax = f2_fma(dx, s, ax);
+    ay = f2_fma(dy, s, ay);
+    az = f2_fma(dz, s, az);
+}
+
+// One interaction, scalar FP32 pipe.
+__device__ __forceinline__ void pair_interact1(float sx, float sy, float sz, float sm,
+                                               float x, float y, float z, float eps2,
+                                               float &ax, float &ay, float &az) {
+    float dx = sx - x, dy = sy - y, dz = sz - z;
+    float d2 = fmaf(dx, dx, eps2);
+    d2 = fmaf(dy, dy, d2);
+    d2 = fmaf(dz, dz, d2);
+    float inv = rsqrt_mufu(d2);
+    float s = (sm * inv) * (inv * inv);
+    ax = fmaf(dx, s, ax);
+    ay = fmaf(dy, s, ay);
+    az = fmaf(dz, s, az);
+}
+
+// Knuth TwoSum: s + e == a + b exactly (round-to-nearest, no FTZ hazards for
+// the magnitudes involved).  __fadd_rn / __fsub_rn keep the compiler from
+// reassociating.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    float aa = __fsub_rn(s, bb);
+    e = __fadd_rn(__fsub_rn(a, aa), __fsub_rn(b, bb));
+}
+
+// Running compensated sum (hi, lo): add t.
+__device__ __forceinline__ void comp_add(float &hi, float &lo, float t) {
+    float s, e;
+    two_sum(hi, t, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+
+// ---------------------------------------------------------------------------
+// mbarrier and 1-D bulk copies (cp.async.bulk, the non-tensor TMA path).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// Global -> shared bulk copy completing on `bar`.  dst, src 16-byte aligned,
+// bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, "
+        "p; }"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for phase `parity` of `bar`, giving up after `limit_ns` nanoseconds.
+// On timeout the status word gets NBGB_STATUS_WAIT_TIMEOUT and false is
+// returned; the caller must leave its loop.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  uint64_t limit_ns = 2000000000ull) {
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        for (int k = 0; k < 64; k++)
+            if (mbar_try_wait(bar, parity))
+                return true;
+        if (global_ns() - t0 > limit_ns) {
+            atomicOr(&g_status, NBGB_STATUS_WAIT_TIMEOUT);
+            return false;
+        }
+    }
+}
+
+}  // namespace nbgb

@@ -1,0 +1,44 @@
+// nbgb_internal.h -- declarations shared between the library's translation
+// units (not part of the public C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace nbgb {
+
+// Largest N any entry point accepts (indices are 32-bit inside the kernels).
+constexpr size_t kMaxBodies = (size_t)1 << 30;
+
+// One force evaluation's decomposition and workspace layout.
+struct ForcePlan {
+    int config = 0;       // index into the kernel configuration table
+    int nsplit = 1;       // j-slices per i-block
+    size_t n = 0;         // bodies
+    int block_bodies = 0; // targets per CTA (BI)
+    int tile_bodies = 0;  // sources per shared-memory tile (JT)
+    int nblocks = 0;      // i-blocks
+    int ntiles = 0;       // j-tiles (the j-stream holds ntiles*JT bodies)
+    size_t ni_pad = 0;    // nblocks * BI
+    size_t off_js = 0, off_hi = 0, off_lo = 0, off_cnt = 0;
+    size_t workspace_bytes = 0;
+};
+
+int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl);
+int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream);
+// jstream == nullptr: use the j-stream inside the workspace.
+int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,
+                 float eps2, void *workspace, cudaStream_t stream);
+int read_and_clear_status(unsigned *bits);
+int launch_integrate_reference(float4 *pm, float4 *vel, const float4 *force, float dt,
+                               float damping, size_t n, float4 *js, int npad, unsigned *counters,
+                               int ncounters, cudaStream_t st);
+int launch_kdk(double *px, double *py, double *pz, double *vx, double *vy, double *vz,
+               const float *mass, const float4 *accel, double kick_dt, double drift_dt,
+               int write_pos, size_t n, float4 *pm, float4 *js, int npad, unsigned *counters,
+               int ncounters, cudaStream_t st);
+const char *config_name(int c);
+int num_configs();
+
+}  // namespace nbgb

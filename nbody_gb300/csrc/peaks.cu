@@ -1,0 +1,146 @@
+// peaks.cu -- microbenchmarks of the pipes the force kernel is bound by,
+// measured on the running GPU so the roofline denominators are this chip's.
+//
+//   fp32 FFMA      scalar fma.rn.f32, 16 independent chains per thread
+//   fp32x2 FFMA2   packed fma.rn.f32x2 (two FMAs per instruction)
+//   MUFU rsqrt     rsqrt.approx.ftz.f32, 16 independent chains per thread
+//
+// FLOP/s counts an FMA as 2 FLOP.  Each kernel runs a full GPU of resident
+// warps (SMs x 8 CTAs x 256 threads) and is timed with CUDA events after a
+// warm-up launch; the best of `reps` launches is reported.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "nbgb_device.cuh"
+#include "nbody_gb300.h"
+
+namespace nbgb {
+
+constexpr int kChains = 16;
+
+__global__ void __launch_bounds__(256) peak_ffma_kernel(float *out, int iters, float a, float b) {
+    float x[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        x[c] = (float)(threadIdx.x + c);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int c = 0; c < kChains; c++)
+                asm volatile("fma.rn.f32 %0, %0, %1, %2;" : "+f"(x[c]) : "f"(a), "f"(b));
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        s += x[c];
+    if (s == 1234.5f)
+        out[threadIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(256) peak_ffma2_kernel(float *out, int iters, float a, float b) {
+    f2 x[kChains];
+    const f2 aa = f2_pack(a, a), bb = f2_pack(b, b);
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        x[c] = f2_pack((float)threadIdx.x, (float)c);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int c = 0; c < kChains; c++)
+                asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(x[c]) : "l"(aa), "l"(bb));
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < kChains; c++) {
+        float l, h;
+        f2_unpack(x[c], l, h);
+        s += l + h;
+    }
+    if (s == 1234.5f)
+        out[threadIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(256) peak_mufu_kernel(float *out, int iters) {
+    float x[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        x[c] = 1.0f + (float)(threadIdx.x + c);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int c = 0; c < kChains; c++)
+                asm volatile("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(x[c]));
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        s += x[c];
+    if (s == 1234.5f)
+        out[threadIdx.x] = s;
+}
+
+}  // namespace nbgb
+
+extern "C" {
+
+// which: 0 = FFMA (FLOP/s), 1 = FFMA2 (FLOP/s), 2 = MUFU rsqrt (ops/s).
+// Result in *rate; *ms = best launch time.  Synchronous.
+NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms_out) {
+    if (which < 0 || which > 2 || iters <= 0 || reps <= 0 || !rate)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    float *out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = NBGB_ERR_CUDA;
+    const dim3 grid(sms * 8), block(256);
+    float best = 1e30f;
+    if (cudaMalloc(&out, 256 * sizeof(float)) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        goto done;
+    for (int r = -1; r < reps; r++) {  // r = -1: warm-up
+        cudaEventRecord(e0, nullptr);
+        if (which == 0)
+            nbgb::peak_ffma_kernel<<<grid, block>>>(out, iters, 0.999f, 1e-3f);
+        else if (which == 1)
+            nbgb::peak_ffma2_kernel<<<grid, block>>>(out, iters, 0.999f, 1e-3f);
+        else
+            nbgb::peak_mufu_kernel<<<grid, block>>>(out, iters);
+        cudaEventRecord(e1, nullptr);
+        if (cudaEventSynchronize(e1) != cudaSuccess)
+            goto done;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r >= 0 && ms < best)
+            best = ms;
+    }
+    {
+        const double threads = (double)grid.x * block.x;
+        const double per_thread = (double)iters * 8 * nbgb::kChains;
+        double ops = threads * per_thread;
+        if (which == 0)
+            ops *= 2.0;  // FMA = 2 FLOP
+        else if (which == 1)
+            ops *= 4.0;  // two FMAs per instruction
+        *rate = ops / (best * 1e-3);
+        if (ms_out)
+            *ms_out = best;
+        rc = NBGB_OK;
+    }
+done:
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    cudaFree(out);
+    return rc;
+}
+
+}  // extern "C"

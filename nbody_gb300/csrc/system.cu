@@ -1,0 +1,438 @@
+// system.cu -- a GPU-resident simulation: the reference's per-step
+// orchestration (src/nbody.cu:293-470: force pass, then integrate) without
+// the host round trip.
+//
+// The reference copies posMass host->device, runs the force algorithm,
+// copies forces back and integrates on one host thread every step
+// (src/nbody.cu:351-371, 420-441).  Here state stays in HBM: a step is one
+// force launch plus one integrate launch that also writes the next step's
+// j-stream, captured once into a CUDA graph and replayed.
+//
+// Two integrators:
+//   NBGB_INTEGRATOR_REFERENCE  integrateOne (src/nbody.cu:158-182), FP32,
+//                              damping, invMass from velInvMass.w
+//   NBGB_INTEGRATOR_KDK64      FP64 kick-drift-kick leapfrog, a = F, no damping
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "nbgb_internal.h"
+#include "nbody_gb300.h"
+
+using nbgb::ForcePlan;
+
+struct nbgb_system {
+    size_t n = 0;
+    int integrator = 0;
+    float eps2 = 0.f, dt = 0.f, damping = 1.f;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    ForcePlan plan;
+    // device state
+    float4 *pm = nullptr;     // posMass {x,y,z,m} (FP32, what the force pass reads)
+    float4 *vel = nullptr;    // velInvMass {vx,vy,vz,1/m} (reference integrator)
+    float4 *force = nullptr;  // force / acceleration {fx,fy,fz,0}
+    double *x64 = nullptr;    // KDK: px,py,pz,vx,vy,vz (6 * n doubles)
+    float *mass = nullptr;    // KDK: m
+    void *ws = nullptr;
+    bool js_valid = false;     // j-stream in ws matches pm
+    bool accel_valid = false;  // KDK: force holds a(x) for the current x
+    bool use_graph = true;
+    cudaGraphExec_t graph = nullptr;
+    // optional per-launch timing of the force kernel (bypasses the graph)
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed_once = false;
+    int status = NBGB_OK;
+};
+
+namespace {
+
+float4 *js_of(nbgb_system *s) { return (float4 *)((char *)s->ws + s->plan.off_js); }
+unsigned *cnt_of(nbgb_system *s) {
+    return s->plan.nsplit > 1 ? (unsigned *)((char *)s->ws + s->plan.off_cnt) : nullptr;
+}
+int ncnt_of(nbgb_system *s) { return s->plan.nsplit > 1 ? s->plan.nblocks : 0; }
+int npad_of(nbgb_system *s) { return s->plan.ntiles * s->plan.tile_bodies; }
+
+double *comp(nbgb_system *s, int c) { return s->x64 + (size_t)c * s->n; }
+
+int ensure_jstream(nbgb_system *s) {
+    if (s->js_valid)
+        return NBGB_OK;
+    int rc = nbgb::launch_pack(s->plan, s->pm, s->ws, s->stream);
+    if (rc == NBGB_OK)
+        s->js_valid = true;
+    return rc;
+}
+
+int force_pass(nbgb_system *s) {
+    int rc = ensure_jstream(s);
+    if (rc != NBGB_OK)
+        return rc;
+    return nbgb::launch_force(s->plan, s->force, s->pm, js_of(s), s->eps2, s->ws, s->stream);
+}
+
+// The force launch of a step, bracketed by events when timing is on.
+int timed_force(nbgb_system *s) {
+    if (s->timing && cudaEventRecord(s->ev0, s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    int rc = nbgb::launch_force(s->plan, s->force, s->pm, js_of(s), s->eps2, s->ws, s->stream);
+    if (rc == NBGB_OK && s->timing) {
+        if (cudaEventRecord(s->ev1, s->stream) != cudaSuccess)
+            return NBGB_ERR_CUDA;
+        s->timed_once = true;
+    }
+    return rc;
+}
+
+// One reference step: force(x) then integrate (writes x' and its j-stream).
+int ref_step_body(nbgb_system *s) {
+    int rc = timed_force(s);
+    if (rc != NBGB_OK)
+        return rc;
+    return nbgb::launch_integrate_reference(s->pm, s->vel, s->force, s->dt, s->damping, s->n,
+                                            js_of(s), npad_of(s), cnt_of(s), ncnt_of(s),
+                                            s->stream);
+}
+
+// One fused leapfrog body: v += a*kick; x += v*dt; a = F(x).
+int kdk_body(nbgb_system *s, double kick) {
+    int rc = nbgb::launch_kdk(comp(s, 0), comp(s, 1), comp(s, 2), comp(s, 3), comp(s, 4),
+                              comp(s, 5), s->mass, s->force, kick, (double)s->dt, 1, s->n, s->pm,
+                              js_of(s), npad_of(s), cnt_of(s), ncnt_of(s), s->stream);
+    if (rc != NBGB_OK)
+        return rc;
+    return timed_force(s);
+}
+
+int half_kick(nbgb_system *s) {
+    return nbgb::launch_kdk(comp(s, 0), comp(s, 1), comp(s, 2), comp(s, 3), comp(s, 4), comp(s, 5),
+                            s->mass, s->force, 0.5 * (double)s->dt, 0.0, 0, s->n, s->pm, nullptr, 0,
+                            nullptr, 0, s->stream);
+}
+
+int check_device_status() {
+    unsigned bits = 0;
+    if (nbgb::read_and_clear_status(&bits) != NBGB_OK)
+        return NBGB_ERR_CUDA;
+    return bits ? NBGB_ERR_DEVICE : NBGB_OK;
+}
+
+void free_all(nbgb_system *s) {
+    if (s->graph)
+        cudaGraphExecDestroy(s->graph);
+    if (s->ev0)
+        cudaEventDestroy(s->ev0);
+    if (s->ev1)
+        cudaEventDestroy(s->ev1);
+    cudaFree(s->pm);
+    cudaFree(s->vel);
+    cudaFree(s->force);
+    cudaFree(s->x64);
+    cudaFree(s->mass);
+    cudaFree(s->ws);
+    if (s->stream)
+        cudaStreamDestroy(s->stream);
+}
+
+// Capture one step body into a graph (reference: force+integrate; KDK: full
+// kick + drift + force).
+int build_graph(nbgb_system *s) {
+    if (s->graph)
+        return NBGB_OK;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    int rc = (s->integrator == NBGB_INTEGRATOR_REFERENCE) ? ref_step_body(s)
+                                                          : kdk_body(s, (double)s->dt);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (rc != NBGB_OK || e != cudaSuccess) {
+        if (g)
+            cudaGraphDestroy(g);
+        return NBGB_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    return e == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+NBGB_API nbgb_system *nbgb_system_create(size_t N, int integrator, float softeningSquared, float dt,
+                                         float damping) {
+    if (N == 0 || N > nbgb::kMaxBodies)
+        return nullptr;
+    if (integrator != NBGB_INTEGRATOR_REFERENCE && integrator != NBGB_INTEGRATOR_KDK64)
+        return nullptr;
+    nbgb_system *s = new (std::nothrow) nbgb_system();
+    if (!s)
+        return nullptr;
+    s->n = N;
+    s->integrator = integrator;
+    s->eps2 = softeningSquared;
+    s->dt = dt;
+    s->damping = damping;
+    cudaGetDevice(&s->device);
+    bool ok = nbgb::plan_force(N, -1, -1, s->plan) == NBGB_OK;
+    ok = ok && cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->pm, N * 16) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->force, N * 16) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->ws, s->plan.workspace_bytes) == cudaSuccess;
+    if (integrator == NBGB_INTEGRATOR_REFERENCE) {
+        ok = ok && cudaMalloc(&s->vel, N * 16) == cudaSuccess;
+    } else {
+        ok = ok && cudaMalloc(&s->x64, N * 6 * sizeof(double)) == cudaSuccess;
+        ok = ok && cudaMalloc(&s->mass, N * sizeof(float)) == cudaSuccess;
+    }
+    ok = ok && cudaMemsetAsync(s->force, 0, N * 16, s->stream) == cudaSuccess;
+    // counters start at zero; every force launch leaves them at zero
+    ok = ok && cudaMemsetAsync(s->ws, 0, s->plan.workspace_bytes, s->stream) == cudaSuccess;
+    ok = ok && cudaStreamSynchronize(s->stream) == cudaSuccess;
+    if (!ok) {
+        free_all(s);
+        delete s;
+        return nullptr;
+    }
+    return s;
+}
+
+NBGB_API void nbgb_system_destroy(nbgb_system *s) {
+    if (!s)
+        return;
+    cudaStreamSynchronize(s->stream);
+    free_all(s);
+    delete s;
+}
+
+NBGB_API int nbgb_system_set_graph(nbgb_system *s, int enable) {
+    if (!s)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    s->use_graph = enable != 0;
+    return NBGB_OK;
+}
+
+// Host arrays, float4 AOS: posMass {x,y,z,m}, velInvMass {vx,vy,vz,1/m}.
+// For the KDK integrator velInvMass.w is ignored and positions/velocities
+// are widened to FP64.
+NBGB_API int nbgb_system_set_state(nbgb_system *s, const float *posMass, const float *velInvMass) {
+    if (!s || !posMass || !velInvMass)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const size_t n = s->n;
+    if (cudaMemcpyAsync(s->pm, posMass, n * 16, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    if (s->integrator == NBGB_INTEGRATOR_REFERENCE) {
+        if (cudaMemcpyAsync(s->vel, velInvMass, n * 16, cudaMemcpyHostToDevice, s->stream) !=
+            cudaSuccess)
+            return NBGB_ERR_CUDA;
+    } else {
+        std::vector<double> h(n * 6);
+        std::vector<float> m(n);
+        for (size_t i = 0; i < n; i++) {
+            for (int c = 0; c < 3; c++) {
+                h[c * n + i] = posMass[4 * i + c];
+                h[(3 + c) * n + i] = velInvMass[4 * i + c];
+            }
+            m[i] = posMass[4 * i + 3];
+        }
+        if (cudaMemcpyAsync(s->x64, h.data(), n * 6 * sizeof(double), cudaMemcpyHostToDevice,
+                            s->stream) != cudaSuccess ||
+            cudaMemcpyAsync(s->mass, m.data(), n * sizeof(float), cudaMemcpyHostToDevice,
+                            s->stream) != cudaSuccess ||
+            cudaStreamSynchronize(s->stream) != cudaSuccess)
+            return NBGB_ERR_CUDA;
+    }
+    s->js_valid = false;
+    s->accel_valid = false;
+    return NBGB_OK;
+}
+
+// FP64 state in (KDK only): x, v as double[N][3] (AOS), mass float[N].
+NBGB_API int nbgb_system_set_state64(nbgb_system *s, const double *pos3, const double *vel3,
+                                     const float *mass) {
+    if (!s || !pos3 || !vel3 || !mass || s->integrator != NBGB_INTEGRATOR_KDK64)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const size_t n = s->n;
+    std::vector<double> h(n * 6);
+    std::vector<float> pm(n * 4);
+    for (size_t i = 0; i < n; i++) {
+        for (int c = 0; c < 3; c++) {
+            h[c * n + i] = pos3[3 * i + c];
+            h[(3 + c) * n + i] = vel3[3 * i + c];
+            pm[4 * i + c] = (float)pos3[3 * i + c];
+        }
+        pm[4 * i + 3] = mass[i];
+    }
+    if (cudaMemcpyAsync(s->x64, h.data(), n * 6 * sizeof(double), cudaMemcpyHostToDevice,
+                        s->stream) != cudaSuccess ||
+        cudaMemcpyAsync(s->mass, mass, n * sizeof(float), cudaMemcpyHostToDevice, s->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(s->pm, pm.data(), n * 16, cudaMemcpyHostToDevice, s->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    s->js_valid = false;
+    s->accel_valid = false;
+    return NBGB_OK;
+}
+
+NBGB_API int nbgb_system_step(nbgb_system *s, int nsteps) {
+    if (!s || nsteps < 0)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (nsteps == 0)
+        return NBGB_OK;
+    int rc = ensure_jstream(s);
+    if (rc != NBGB_OK)
+        return rc;
+    const bool graph = s->use_graph && !s->timing;
+    if (s->integrator == NBGB_INTEGRATOR_REFERENCE) {
+        if (graph && (rc = build_graph(s)) != NBGB_OK)
+            return rc;
+        for (int k = 0; k < nsteps; k++) {
+            if (graph) {
+                if (cudaGraphLaunch(s->graph, s->stream) != cudaSuccess)
+                    return NBGB_ERR_CUDA;
+            } else if ((rc = ref_step_body(s)) != NBGB_OK) {
+                return rc;
+            }
+        }
+        return NBGB_OK;
+    }
+    // KDK: v(n) synchronised at entry and exit.
+    if (!s->accel_valid) {
+        if ((rc = force_pass(s)) != NBGB_OK)
+            return rc;
+        s->accel_valid = true;
+    }
+    if ((rc = kdk_body(s, 0.5 * (double)s->dt)) != NBGB_OK)  // first half kick + drift + force
+        return rc;
+    if (nsteps > 1 && graph && (rc = build_graph(s)) != NBGB_OK)
+        return rc;
+    for (int k = 1; k < nsteps; k++) {
+        if (graph) {
+            if (cudaGraphLaunch(s->graph, s->stream) != cudaSuccess)
+                return NBGB_ERR_CUDA;
+        } else if ((rc = kdk_body(s, (double)s->dt)) != NBGB_OK) {
+            return rc;
+        }
+    }
+    return half_kick(s);
+}
+
+// Timing mode: every force launch is bracketed by CUDA events on the
+// system's stream (steps run eagerly, not from the graph).
+NBGB_API int nbgb_system_set_timing(nbgb_system *s, int enable) {
+    if (!s)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (enable && !s->ev0) {
+        if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess)
+            return NBGB_ERR_CUDA;
+    }
+    s->timing = enable != 0;
+    s->timed_once = false;
+    return NBGB_OK;
+}
+
+// Milliseconds of the most recent timed force launch (waits for it).
+NBGB_API int nbgb_system_last_force_ms(nbgb_system *s, float *ms) {
+    if (!s || !ms || !s->timing || !s->timed_once)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (cudaEventSynchronize(s->ev1) != cudaSuccess ||
+        cudaEventElapsedTime(ms, s->ev0, s->ev1) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    return NBGB_OK;
+}
+
+NBGB_API int nbgb_system_synchronize(nbgb_system *s) {
+    if (!s)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    return check_device_status();
+}
+
+NBGB_API int nbgb_system_get_state(nbgb_system *s, float *posMass, float *velInvMass) {
+    if (!s)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const size_t n = s->n;
+    if (posMass &&
+        cudaMemcpyAsync(posMass, s->pm, n * 16, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    if (velInvMass) {
+        if (s->integrator == NBGB_INTEGRATOR_REFERENCE) {
+            if (cudaMemcpyAsync(velInvMass, s->vel, n * 16, cudaMemcpyDeviceToHost, s->stream) !=
+                cudaSuccess)
+                return NBGB_ERR_CUDA;
+        } else {
+            std::vector<double> h(n * 3);
+            std::vector<float> m(n);
+            if (cudaMemcpyAsync(h.data(), comp(s, 3), n * 3 * sizeof(double),
+                                cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
+                cudaMemcpyAsync(m.data(), s->mass, n * sizeof(float), cudaMemcpyDeviceToHost,
+                                s->stream) != cudaSuccess ||
+                cudaStreamSynchronize(s->stream) != cudaSuccess)
+                return NBGB_ERR_CUDA;
+            for (size_t i = 0; i < n; i++) {
+                for (int c = 0; c < 3; c++)
+                    velInvMass[4 * i + c] = (float)h[c * n + i];
+                velInvMass[4 * i + 3] = 1.0f / m[i];
+            }
+        }
+    }
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    return check_device_status();
+}
+
+NBGB_API int nbgb_system_get_state64(nbgb_system *s, double *pos3, double *vel3) {
+    if (!s || s->integrator != NBGB_INTEGRATOR_KDK64)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const size_t n = s->n;
+    std::vector<double> h(n * 6);
+    if (cudaMemcpyAsync(h.data(), s->x64, n * 6 * sizeof(double), cudaMemcpyDeviceToHost,
+                        s->stream) != cudaSuccess ||
+        cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    for (size_t i = 0; i < n; i++)
+        for (int c = 0; c < 3; c++) {
+            if (pos3)
+                pos3[3 * i + c] = h[c * n + i];
+            if (vel3)
+                vel3[3 * i + c] = h[(3 + c) * n + i];
+        }
+    return check_device_status();
+}
+
+// Forces of the last force pass (reference: F(x) before the integrate; KDK:
+// a(x) at the current positions), float4 AOS.
+NBGB_API int nbgb_system_get_force(nbgb_system *s, float *force) {
+    if (!s || !force)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (cudaMemcpyAsync(force, s->force, s->n * 16, cudaMemcpyDeviceToHost, s->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    return check_device_status();
+}
+
+// Device pointers for callers that manage copies themselves.
+NBGB_API void *nbgb_system_device_posmass(nbgb_system *s) { return s ? s->pm : nullptr; }
+NBGB_API void *nbgb_system_device_force(nbgb_system *s) { return s ? s->force : nullptr; }
+NBGB_API void *nbgb_system_stream(nbgb_system *s) { return s ? s->stream : nullptr; }
+NBGB_API int nbgb_system_plan(nbgb_system *s, int *config, int *nsplit) {
+    if (!s)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (config)
+        *config = s->plan.config;
+    if (nsplit)
+        *nsplit = s->plan.nsplit;
+    return NBGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+"""Pins the CPU oracle to the reference's own outputs (tests/golden/, made by
+the reference's compiled CPU_AOS / CPU_SOA / randomUnitBodies objects)."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_FORCE_CASES, golden
+from oracle import oracle as O
+
+# Per-body norm-wise tolerance of an FP32 all-pairs force against the
+# reference's CPU_AOS (spec accuracy gate).
+FORCE_TOL = 1e-5
+
+
+@pytest.mark.parametrize("case", GOLDEN_FORCE_CASES)
+def test_restatement_matches_reference_forces(case):
+    g = golden(case)
+    pm, eps2 = g["posMass"], float(g["eps2"])
+    for impl in (O.ieee(), O.fast()):
+        f = impl.forces_aos(pm, eps2)
+        mx, rms = O.per_body_rel_error(f, g["force_aos"])
+        assert mx <= FORCE_TOL, (case, mx, rms)
+    f = O.fast().forces_soa(pm, eps2)
+    assert O.per_body_rel_error(f, g["force_aos"])[0] <= FORCE_TOL
+
+
+@pytest.mark.parametrize("case", GOLDEN_FORCE_CASES)
+def test_fp64_oracle_matches_reference(case):
+    g = golden(case)
+    f = O.ieee().forces_f64(g["posMass"], float(g["eps2"]))
+    ref = g["force_aos"].astype(np.float64)[:, :3]
+    num = np.linalg.norm(ref - f, axis=1)
+    den = np.linalg.norm(f, axis=1)
+    assert (num / den).max() <= FORCE_TOL
+    # the stored FP64 forces are this oracle's (regression guard)
+    np.testing.assert_allclose(f, g["force_f64"][:, :3], rtol=0, atol=0)
+
+
+def test_reference_aos_and_soa_agree():
+    g = golden("ball2048")
+    assert np.array_equal(g["force_aos"][:, :3], g["force_soa"][:, :3])
+
+
+def test_reference_initial_conditions_exact():
+    g = golden("refic1024_seed7")
+    pos, vel = O.ieee().random_unit_bodies(1024, 7, 0.9, 8.0)
+    assert np.array_equal(pos, g["posMass"])
+    assert np.array_equal(vel, g["velInvMass"])
+
+
+def test_integrator_restatement_reproduces_trajectory_step():
+    t = golden("traj1024")
+    p, v = t["posMass0"].copy(), t["velInvMass0"].copy()
+    f = t["force_step1"].copy()
+    O.ieee().integrate(p, v, f, float(t["dt"]), float(t["damping"]))
+    assert np.array_equal(p, t["posMass1"])
+    assert np.array_equal(v, t["velInvMass1"])
+
+
+def test_crosscheck_metric_semantics():
+    # relError(a, b) = |a-b|/b with signed b: negative-golden components never
+    # raise the maximum (src/nbody.cu:120-125)
+    g = np.zeros((2, 4), np.float32)
+    f = np.zeros((2, 4), np.float32)
+    g[0, :3] = [1.0, -1.0, 2.0]
+    f[0, :3] = [1.1, -2.0, 2.0]
+    g[1, :3] = [4.0, 0.0, 0.0]
+    f[1, :3] = [4.0, 0.0, 0.0]
+    f[1, 3] = 99.0  # w is ignored
+    e = O.ieee().max_rel_error(f, g)
+    assert abs(e - 0.1) < 1e-6

@@ -1,0 +1,122 @@
+"""Device-resident step loop: the reference's crosscheck applied every step
+(forces on identical positions, src/nbody.cu:313-325, 406-418), the fused
+integrate bit-exact, and whole trajectories within the spread that the
+reference's own CPU variants show."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import oracle as O
+
+import nbody_gb300 as nb
+
+pytestmark = pytest.mark.gpu
+
+TOL_FORCE = 1e-5
+
+
+def _rel_pos(a, b):
+    a = np.asarray(a, np.float64)[:, :3]
+    b = np.asarray(b, np.float64)[:, :3]
+    return np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
+
+
+def test_plain_case_ten_steps_crosschecked_every_step(cuda):
+    """N = 16,384 unit ball, m = 1/N, v = 0, eps2 = 1e-4, dt = 0.01, 10 steps."""
+    n = 16384
+    pm0, vm0 = nb.ic_uniform_ball(n, 16384)
+    sysm = nb.System(n, nb.INTEGRATOR_REFERENCE, 1e-4, 0.01, 0.95)
+    sysm.set_state(pm0, vm0)
+    for step in range(10):
+        p_before, v_before = sysm.get_state()
+        sysm.step(1)
+        f_gpu = sysm.get_force()
+        f_ref = O.fast().forces_aos(p_before, 1e-4)
+        mx, _ = O.per_body_rel_error(f_gpu, f_ref)
+        assert mx <= TOL_FORCE, (step, mx)
+        # the fused integrate on the GPU forces: bit-exact
+        O.ieee().integrate(p_before, v_before, f_gpu, 0.01, 0.95)
+        p_after, v_after = sysm.get_state()
+        assert np.array_equal(p_after, p_before) and np.array_equal(v_after, v_before)
+    sysm.close()
+
+
+def test_plain_case_trajectory_within_reference_spread(cuda):
+    """Free-running 10-step trajectory against the oracle-driven one.  The
+    reference's integrator multiplies the acceleration by 1/m = N, so
+    rounding differences grow quickly; the reference's own CPU variants
+    (CPU_AOS vs an IEEE restatement) differ at step 10 by median 2.4e-5,
+    p99 2.4e-3 per body.  Bounds: step 1 max 1e-4; step 10 median 1e-4,
+    p99 1e-2."""
+    n = 16384
+    pm0, vm0 = nb.ic_uniform_ball(n, 16384)
+    sysm = nb.System(n, nb.INTEGRATOR_REFERENCE, 1e-4, 0.01, 0.95)
+    sysm.set_state(pm0, vm0)
+    p, v = pm0.copy(), vm0.copy()
+    for step in range(1, 11):
+        sysm.step(1)
+        f = O.fast().forces_aos(p, 1e-4)
+        O.ieee().integrate(p, v, f, 0.01, 0.95)
+        g, _ = sysm.get_state()
+        rel = _rel_pos(g, p)
+        if step == 1:
+            assert rel.max() <= 1e-4
+    assert np.median(rel) <= 1e-4 and np.quantile(rel, 0.99) <= 1e-2
+    sysm.close()
+
+
+def test_golden_trajectory(cuda):
+    t = golden("traj1024")
+    sysm = nb.System(1024, nb.INTEGRATOR_REFERENCE, float(t["eps2"]), float(t["dt"]),
+                     float(t["damping"]))
+    sysm.set_state(t["posMass0"], t["velInvMass0"])
+    sysm.step(1)
+    p1, _ = sysm.get_state()
+    assert _rel_pos(p1, t["posMass1"]).max() <= 1e-4
+    sysm.step(4)
+    p5, _ = sysm.get_state()
+    sysm.step(5)
+    p10, _ = sysm.get_state()
+    for p, ref in ((p5, t["posMass5"]), (p10, t["posMass10"])):
+        rel = _rel_pos(p, ref)
+        assert np.median(rel) <= 1e-4 and np.quantile(rel, 0.99) <= 1e-2
+    sysm.close()
+
+
+def test_graph_and_eager_steps_identical(cuda):
+    pm0, vm0 = nb.ic_reference(4096, 7)
+    out = []
+    for graph in (True, False):
+        s = nb.System(4096, nb.INTEGRATOR_REFERENCE, 0.01, 0.016, 0.95)
+        s.use_graph(graph)
+        s.set_state(pm0, vm0)
+        s.step(7)
+        out.append(s.get_state())
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_kdk64_conserves_energy_small(cuda):
+    """FP64 leapfrog on a 2,048-body Plummer sphere: energy drift over 200
+    steps at dt = 0.002 stays small (FP64 energy from the oracle)."""
+    n = 2048
+    p, v, pm, _ = nb.ic_plummer(n, 3)
+    m = pm[:, 3].copy()
+    s = nb.System(n, nb.INTEGRATOR_KDK64, 1e-4, 0.002, 1.0)
+    s.set_state64(p, v, m)
+
+    def energy(pos, vel):
+        pm4 = np.zeros((n, 4), np.float32)
+        pm4[:, :3] = pos
+        pm4[:, 3] = m
+        phi = O.ieee().potential_f64(pm4, float(np.float32(1e-4)))
+        return 0.5 * (m * (vel ** 2).sum(1)).sum() + 0.5 * (m * phi).sum()
+
+    e0 = energy(p, v)
+    s.step(200)
+    p1, v1 = s.get_state64()
+    e1 = energy(p1, v1)
+    assert abs(e1 - e0) / abs(e0) < 1e-4
+    # momentum stays ~0
+    assert np.abs((m[:, None] * v1).sum(0)).max() < 1e-6
+    s.close()
