@@ -233,7 +233,7 @@ def run_gb300(args, ws, rank, local):
     mufu, _ = nb.measure_peak("mufu")
     fp32_peak = max(ffma, ffma2)
 
-    n = N_BODIES
+    n = args.n
     p3, v3, pm_np, _ = nb.ic_plummer(n, SEED + rank)
     sysm = nb.System(n, nb.INTEGRATOR_KDK64, EPS2, DT, 1.0)
     sysm.set_state64(p3, v3, pm_np[:, 3].copy())
@@ -306,7 +306,7 @@ def run_gb300(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Plummer sphere, G=M=a=1)",
-        "config": {"workload": "plain large system: N=1,048,576 Plummer, FP32 force, "
+        "config": {"workload": f"plain large system: N={n:,} Plummer, FP32 force, "
                                "FP64 KDK integrate, eps2=1e-4, dt=0.005",
                    "n_bodies": n, "integrator": "kdk64", "force_config":
                        nb.force_config_names()[cfg], "nsplit": nsplit,
@@ -341,6 +341,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--n", type=int, default=N_BODIES,
+                    help="bodies (default 1,048,576; smaller only for profiling captures)")
     args = ap.parse_args()
     ws, rank, local = _dist()
     if args.impl == "reference":

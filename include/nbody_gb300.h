@@ -168,8 +168,10 @@ NBGB_API int nbgb_force_error_stats(const float *force, const double *truth3,
 /* ======================================================================== */
 
 /* which: 0 = scalar FP32 FMA (FLOP/s, FMA = 2), 1 = packed f32x2 FMA
-   (FLOP/s), 2 = MUFU rsqrt (results/s).  Full-GPU launch of `iters` x 128
-   operations per thread, best of `reps` after a warm-up.  Synchronous. */
+   (FLOP/s), 2 = MUFU rsqrt (results/s), 3 = packed add, 4 = packed multiply
+   (FLOP/s, 2 per instruction), 5 = packed FMA with three varying register
+   operands.  Full-GPU launch of `iters` x 128 operations per thread, best of
+   `reps` after a warm-up.  Synchronous. */
 NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms);
 
 /* ======================================================================== */

@@ -143,8 +143,9 @@ def integrate_reference(posMass, velInvMass, force_, dt: float, damping: float, 
 
 
 def measure_peak(which: str, iters: int = 4096, reps: int = 5):
-    """Measured pipe throughput: 'ffma' / 'ffma2' (FLOP/s) or 'mufu' (rsqrt/s)."""
-    code = {"ffma": 0, "ffma2": 1, "mufu": 2}[which]
+    """Measured pipe throughput: 'ffma' / 'ffma2' / 'fadd2' / 'fmul2' /
+    'ffma2_3op' (FLOP/s) or 'mufu' (rsqrt/s)."""
+    code = {"ffma": 0, "ffma2": 1, "mufu": 2, "fadd2": 3, "fmul2": 4, "ffma2_3op": 5}[which]
     rate, ms = ctypes.c_double(), ctypes.c_float()
     check(load().nbgb_measure_peak(code, iters, reps, ctypes.byref(rate), ctypes.byref(ms)),
           "nbgb_measure_peak")

@@ -82,7 +82,7 @@ __global__ void pack_jstream_kernel(const float4 *__restrict__ pm, float4 *__res
 // ---------------------------------------------------------------------------
 // force kernel
 // ---------------------------------------------------------------------------
-template <int W, int K, int JT, int STAGES, bool PACKED, int UNROLL, int MINB>
+template <int W, int K, int JT, int STAGES, int MODE, int UNROLL, int MINB>
 __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     constexpr int NT = W * 32;
     constexpr int BI = NT * K;
@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     }
     const f2 eps2p = f2_pack(p.eps2, p.eps2);
     const f2 zero2 = f2_pack(0.f, 0.f);
+    const f2 one2 = f2_pack(1.f, 1.f);
 
     bool failed = false;
     int t = 0;
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
         const bool ok = mbar_wait_bounded(&full[s], parity);
         if (ok) {
             const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(ring + s * JT);
-            if (PACKED) {
+            if (MODE != 0) {  // packed f32x2 (MODE 2: every op issued as an FMA)
                 f2 ax[K], ay[K], az[K];
 #pragma unroll
                 for (int k = 0; k < K; k++)
@@ -154,9 +155,14 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                     const ulonglong2 a = tp[2 * q];
                     const ulonglong2 b = tp[2 * q + 1];
 #pragma unroll
-                    for (int k = 0; k < K; k++)
-                        pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p, ax[k],
-                                       ay[k], az[k]);
+                    for (int k = 0; k < K; k++) {
+                        if (MODE == 2)
+                            pair_interact2_fma(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p,
+                                               one2, zero2, ax[k], ay[k], az[k]);
+                        else
+                            pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p, ax[k],
+                                           ay[k], az[k]);
+                    }
                 }
 #pragma unroll
                 for (int k = 0; k < K; k++) {
@@ -278,33 +284,50 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
 // ---------------------------------------------------------------------------
 struct ForceConfig {
     int warps, k, jt, stages;
-    bool packed;
+    int mode;  // 0 scalar FP32, 1 packed f32x2, 2 packed with every op as an FMA
     const void *fn;
     const char *name;
 };
 
-// W warps, K targets per thread, JT sources per tile, ST ring stages, packed
-// f32x2 or scalar, inner unroll, minimum resident CTAs (register cap).
+// W warps, K targets per thread, JT sources per tile, ST ring stages, mode
+// (0 scalar, 1 f32x2, 2 f32x2 all-FMA), inner unroll, minimum resident CTAs
+// (register cap).
 #define NBGB_CFG(W, K, JT, ST, PK, UN, MB, PIPE)                                           \
     {W, K, JT, ST, PK, (const void *)force_kernel<W, K, JT, ST, PK, UN, MB>,               \
      "w" #W "_k" #K "_jt" #JT "_s" #ST "_" PIPE}
 
 static const ForceConfig kConfigs[] = {
-    NBGB_CFG(8, 4, 512, 3, true, 4, 2, "f32x2"),  // 0: BI 1024
-    NBGB_CFG(4, 4, 512, 3, true, 4, 4, "f32x2"),  // 1: BI 512
-    NBGB_CFG(8, 2, 256, 4, true, 8, 2, "f32x2"),  // 2: BI 512
-    NBGB_CFG(4, 2, 256, 4, true, 8, 4, "f32x2"),  // 3: BI 256
-    NBGB_CFG(8, 4, 512, 3, false, 4, 2, "f32"),   // 4: scalar FP32 pipe, BI 1024
-    NBGB_CFG(4, 8, 512, 3, true, 2, 2, "f32x2"),  // 5: BI 1024, 8 targets per thread
+    NBGB_CFG(8, 4, 512, 3, 1, 4, 2, "f32x2"),  // 0: BI 1024
+    NBGB_CFG(4, 4, 512, 3, 1, 4, 4, "f32x2"),  // 1: BI 512
+    NBGB_CFG(8, 2, 256, 4, 1, 8, 2, "f32x2"),  // 2: BI 512
+    NBGB_CFG(4, 2, 256, 4, 1, 8, 4, "f32x2"),  // 3: BI 256
+    NBGB_CFG(8, 4, 512, 3, 0, 4, 2, "f32"),   // 4: scalar FP32 pipe, BI 1024
+    NBGB_CFG(4, 8, 512, 3, 1, 2, 2, "f32x2"),  // 5: BI 1024, 8 targets per thread
+    NBGB_CFG(8, 2, 256, 4, 1, 8, 3, "f32x2"),  // 6: as 2, 3 CTAs/SM (<= 85 regs)
+    NBGB_CFG(8, 4, 512, 3, 1, 2, 2, "f32x2"),  // 7: as 0, unroll 2
+    NBGB_CFG(4, 4, 512, 3, 1, 8, 3, "f32x2"),  // 8: as 1, unroll 8
+    NBGB_CFG(16, 2, 256, 4, 1, 8, 1, "f32x2"), // 9: 512 threads
+    NBGB_CFG(8, 2, 256, 4, 1, 4, 2, "f32x2"),  // 10: as 2, unroll 4
+    NBGB_CFG(8, 2, 256, 4, 1, 16, 2, "f32x2"), // 11: as 2, unroll 16
+    NBGB_CFG(8, 2, 256, 4, 0, 8, 3, "f32"),   // 12: scalar, K 2
+    NBGB_CFG(8, 1, 256, 4, 1, 16, 3, "f32x2"), // 13: K 1, 3 CTAs/SM
+    NBGB_CFG(8, 2, 256, 4, 2, 4, 2, "fma2"),   // 14: as 10, all-FMA
+    NBGB_CFG(4, 8, 512, 3, 2, 2, 2, "fma2"),   // 15: as 5, all-FMA
+    NBGB_CFG(8, 2, 256, 4, 2, 8, 2, "fma2"),   // 16: as 2, all-FMA
+    NBGB_CFG(16, 2, 256, 4, 2, 4, 1, "fma2"),  // 17: as 9, all-FMA, unroll 4
 };
 static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
 static const int kDefaultCandidates[] = {0, 1, 2, 3, 5};
 
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+constexpr int kMaxConfigs = 64;
+static_assert(sizeof(kConfigs) / sizeof(kConfigs[0]) <= (size_t)kMaxConfigs,
+              "DeviceInfo::occ must hold every configuration");
+
 struct DeviceInfo {
     int sms = 0;
-    int occ[16] = {0};
+    int occ[kMaxConfigs] = {0};
     bool ok = false;
 };
 

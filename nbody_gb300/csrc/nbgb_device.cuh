@@ -99,6 +99,29 @@ __device__ __forceinline__ void pair_interact2(f2 sx, f2 sy, f2 sz, f2 sm,
     az = f2_fma(dz, s, az);
 }
 
+// As pair_interact2, but every add and multiply is issued as an FMA
+// (a + b = fma(a, 1, b), a * b = fma(a, b, 0)); results are identical because
+// each FMA still rounds once.
+__device__ __forceinline__ void pair_interact2_fma(f2 sx, f2 sy, f2 sz, f2 sm,
+                                                   f2 nx, f2 ny, f2 nz, f2 eps2, f2 one,
+                                                   f2 zero, f2 &ax, f2 &ay, f2 &az) {
+    f2 dx = f2_fma(sx, one, nx);
+    f2 dy = f2_fma(sy, one, ny);
+    f2 dz = f2_fma(sz, one, nz);
+    f2 d2 = f2_fma(dx, dx, eps2);
+    d2 = f2_fma(dy, dy, d2);
+    d2 = f2_fma(dz, dz, d2);
+    float d2l, d2h;
+    f2_unpack(d2, d2l, d2h);
+    f2 inv = f2_pack(rsqrt_mufu(d2l), rsqrt_mufu(d2h));
+    f2 inv2 = f2_fma(inv, inv, zero);
+    f2 s = f2_fma(sm, inv, zero);
+    s = f2_fma(s, inv2, zero);
+    ax = f2_fma(dx, s, ax);
+    ay = f2_fma(dy, s, ay);
+    az = f2_fma(dz, s, az);
+}
+
 // One interaction, scalar FP32 pipe.
 __device__ __forceinline__ void pair_interact1(float sx, float sy, float sz, float sm,
                                                float x, float y, float z, float eps2,

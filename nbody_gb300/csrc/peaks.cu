@@ -63,6 +63,44 @@ __global__ void __launch_bounds__(256) peak_ffma2_kernel(float *out, int iters, 
         out[threadIdx.x] = s;
 }
 
+// Packed add / mul throughput (which = 3 / 4), and FFMA2 with three varying
+// operands (which = 5), for comparison with the FFMA2 rate above.
+template <int OP>
+__global__ void __launch_bounds__(256) peak_f2op_kernel(float *out, int iters, float a, float b) {
+    f2 x[kChains], y[kChains], z[kChains];
+    f2 aa = f2_pack(a, a), bb = f2_pack(b, b);
+#pragma unroll
+    for (int c = 0; c < kChains; c++) {
+        x[c] = f2_pack((float)threadIdx.x, (float)c);
+        y[c] = f2_pack(a - 1e-6f * c, a + 1e-6f * c);
+        z[c] = f2_pack(b * c, b + c);
+    }
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int c = 0; c < kChains; c++) {
+                if (OP == 3)
+                    asm volatile("add.rn.ftz.f32x2 %0, %0, %1;" : "+l"(x[c]) : "l"(bb));
+                else if (OP == 4)
+                    asm volatile("mul.rn.ftz.f32x2 %0, %0, %1;" : "+l"(x[c]) : "l"(aa));
+                else
+                    asm volatile("fma.rn.ftz.f32x2 %0, %0, %1, %2;"
+                                 : "+l"(x[c])
+                                 : "l"(y[c]), "l"(z[(c + 3) % kChains]));
+            }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < kChains; c++) {
+        float l, h;
+        f2_unpack(x[c], l, h);
+        s += l + h;
+    }
+    if (s == 1234.5f)
+        out[threadIdx.x] = s;
+}
+
 __global__ void __launch_bounds__(256) peak_mufu_kernel(float *out, int iters) {
     float x[kChains];
 #pragma unroll
@@ -87,10 +125,12 @@ __global__ void __launch_bounds__(256) peak_mufu_kernel(float *out, int iters) {
 
 extern "C" {
 
-// which: 0 = FFMA (FLOP/s), 1 = FFMA2 (FLOP/s), 2 = MUFU rsqrt (ops/s).
+// which: 0 = FFMA (FLOP/s), 1 = FFMA2 (FLOP/s), 2 = MUFU rsqrt (ops/s),
+//        3 = add.f32x2, 4 = mul.f32x2 (FLOP/s, 2 per instruction), 5 = FFMA2
+//        with three varying operands (FLOP/s).
 // Result in *rate; *ms = best launch time.  Synchronous.
 NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms_out) {
-    if (which < 0 || which > 2 || iters <= 0 || reps <= 0 || !rate)
+    if (which < 0 || which > 5 || iters <= 0 || reps <= 0 || !rate)
         return NBGB_ERR_INVALID_ARGUMENT;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -111,8 +151,14 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
             nbgb::peak_ffma_kernel<<<grid, block>>>(out, iters, 0.999f, 1e-3f);
         else if (which == 1)
             nbgb::peak_ffma2_kernel<<<grid, block>>>(out, iters, 0.999f, 1e-3f);
-        else
+        else if (which == 2)
             nbgb::peak_mufu_kernel<<<grid, block>>>(out, iters);
+        else if (which == 3)
+            nbgb::peak_f2op_kernel<3><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
+        else if (which == 4)
+            nbgb::peak_f2op_kernel<4><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
+        else
+            nbgb::peak_f2op_kernel<5><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
         cudaEventRecord(e1, nullptr);
         if (cudaEventSynchronize(e1) != cudaSuccess)
             goto done;
@@ -127,8 +173,10 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
         double ops = threads * per_thread;
         if (which == 0)
             ops *= 2.0;  // FMA = 2 FLOP
-        else if (which == 1)
+        else if (which == 1 || which == 5)
             ops *= 4.0;  // two FMAs per instruction
+        else if (which == 3 || which == 4)
+            ops *= 2.0;  // two adds / multiplies per instruction
         *rate = ops / (best * 1e-3);
         if (ms_out)
             *ms_out = best;

@@ -14,8 +14,12 @@ pytestmark = pytest.mark.gpu
 
 # Per-body |F - F_ref| / |F_ref| against the reference's CPU_AOS (north-star
 # accuracy gate), and against the FP64 all-pairs sum of the same FP32 inputs.
+# On the golden fixtures the reference's own CPU_AOS is up to 1.8e-6 (RMS
+# 1.7e-7) from FP64 and a sequential IEEE binary32 sum up to 3.1e-6 (RMS
+# 9.6e-7); the bounds below sit above both.
 TOL_VS_REFERENCE = 1e-5
-TOL_VS_FP64 = 2e-6
+TOL_VS_FP64 = 5e-6
+RMS_VS_FP64 = 1e-6
 
 
 def _gpu_force(pm_np, eps2, config=-1, nsplit=-1):
@@ -47,14 +51,14 @@ def test_drop_in_entry_matches_reference(cuda, case):
     assert np.all(out[:, 3] == 0.0)
     mx, rms = O.per_body_rel_error(out, g["force_aos"])
     assert mx <= TOL_VS_REFERENCE, (mx, rms)
-    mx64, _ = O.per_body_rel_error(out, g["force_f64"])
-    assert mx64 <= TOL_VS_FP64
+    mx64, rms64 = O.per_body_rel_error(out, g["force_f64"])
+    assert mx64 <= TOL_VS_FP64 and rms64 <= RMS_VS_FP64
     # the reference's own crosscheck metric is reported, not asserted, by the
     # reference (src/nbody.cu:1049-1050); same here, but it must be finite
     assert np.isfinite(nb.crosscheck_max_rel_error(out, g["force_aos"]))
 
 
-@pytest.mark.parametrize("config", range(6))
+@pytest.mark.parametrize("config", range(18))
 @pytest.mark.parametrize("nsplit", [1, 2, 3, 7])
 def test_every_configuration_and_split(cuda, config, nsplit):
     g = golden("plummer4096")
@@ -80,11 +84,11 @@ def test_plain_16k_case(cuda):
     n = 16384
     pm, _ = nb.ic_uniform_ball(n, 16384)
     out = _gpu_force(pm, 1e-4)
-    ref = O.fast().forces_aos(pm, 1e-4)
+    ref = O.ieee().forces_aos(pm, 1e-4)
     assert O.per_body_rel_error(out, ref)[0] <= TOL_VS_REFERENCE
     idx = np.random.default_rng(0).choice(n, 2048, replace=False)
     mx, rms = nb.force_error_stats(out, _f64_as4(pm, 1e-4, idx)[:, :3], idx)
-    assert mx <= TOL_VS_FP64 and rms <= 5e-7
+    assert mx <= TOL_VS_FP64 and rms <= RMS_VS_FP64
 
 
 def test_million_body_plummer_properties(cuda):
@@ -95,7 +99,7 @@ def test_million_body_plummer_properties(cuda):
     out = _gpu_force(pm, 1e-4)
     idx = np.random.default_rng(1).choice(n, 512, replace=False)
     mx, rms = nb.force_error_stats(out, _f64_as4(pm, 1e-4, idx)[:, :3], idx)
-    assert mx <= TOL_VS_FP64, (mx, rms)
+    assert mx <= TOL_VS_FP64 and rms <= RMS_VS_FP64, (mx, rms)
     # total momentum change sum_i m_i F_i vanishes (pairwise antisymmetry)
     m = pm[:, 3:4].astype(np.float64)
     tot = (m * out[:, :3]).sum(0)

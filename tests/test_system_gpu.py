@@ -13,6 +13,8 @@ import nbody_gb300 as nb
 pytestmark = pytest.mark.gpu
 
 TOL_FORCE = 1e-5
+# against FP64 on the same FP32 positions (see test_force_gpu.py)
+TOL_VS_FP64 = 5e-6
 
 
 def _rel_pos(a, b):
@@ -22,18 +24,28 @@ def _rel_pos(a, b):
 
 
 def test_plain_case_ten_steps_crosschecked_every_step(cuda):
-    """N = 16,384 unit ball, m = 1/N, v = 0, eps2 = 1e-4, dt = 0.01, 10 steps."""
+    """N = 16,384 unit ball, m = 1/N, v = 0, eps2 = 1e-4, dt = 0.01, 10 steps.
+    Every step the GPU forces are compared on the same positions with an FP64
+    all-pairs sum and with the IEEE binary32 restatement of CPU_AOS: the GPU
+    must be within 5e-6 of FP64 or at least as close as the restatement
+    (whose own error grows as the reference integrator scatters the bodies),
+    and within 1e-5 of the restatement itself."""
     n = 16384
     pm0, vm0 = nb.ic_uniform_ball(n, 16384)
     sysm = nb.System(n, nb.INTEGRATOR_REFERENCE, 1e-4, 0.01, 0.95)
     sysm.set_state(pm0, vm0)
+    eps2 = float(np.float32(1e-4))
     for step in range(10):
         p_before, v_before = sysm.get_state()
         sysm.step(1)
         f_gpu = sysm.get_force()
-        f_ref = O.fast().forces_aos(p_before, 1e-4)
-        mx, _ = O.per_body_rel_error(f_gpu, f_ref)
-        assert mx <= TOL_FORCE, (step, mx)
+        f_ieee = O.ieee().forces_aos(p_before, 1e-4)
+        f64 = np.zeros((n, 4))
+        f64[:, :3] = O.ieee().forces_f64(p_before, eps2)
+        mx, rms = O.per_body_rel_error(f_gpu, f64)
+        mx_i, rms_i = O.per_body_rel_error(f_ieee, f64)
+        assert mx <= max(TOL_VS_FP64, mx_i) and rms <= rms_i, (step, mx, mx_i, rms, rms_i)
+        assert O.per_body_rel_error(f_gpu, f_ieee)[0] <= max(TOL_FORCE, 2 * mx_i), step
         # the fused integrate on the GPU forces: bit-exact
         O.ieee().integrate(p_before, v_before, f_gpu, 0.01, 0.95)
         p_after, v_after = sysm.get_state()
@@ -42,10 +54,12 @@ def test_plain_case_ten_steps_crosschecked_every_step(cuda):
 
 
 def test_plain_case_trajectory_within_reference_spread(cuda):
-    """Free-running 10-step trajectory against the oracle-driven one.  The
+    """Free-running 10-step trajectory against the oracle-driven one (IEEE
+    binary32 restatement; the restatement built with the reference's aarch64
+    flags uses -mlow-precision-recip-sqrt and is itself 6e-5 off).  The
     reference's integrator multiplies the acceleration by 1/m = N, so
     rounding differences grow quickly; the reference's own CPU variants
-    (CPU_AOS vs an IEEE restatement) differ at step 10 by median 2.4e-5,
+    (CPU_AOS vs the IEEE restatement) differ at step 10 by median 2.4e-5,
     p99 2.4e-3 per body.  Bounds: step 1 max 1e-4; step 10 median 1e-4,
     p99 1e-2."""
     n = 16384
@@ -55,7 +69,7 @@ def test_plain_case_trajectory_within_reference_spread(cuda):
     p, v = pm0.copy(), vm0.copy()
     for step in range(1, 11):
         sysm.step(1)
-        f = O.fast().forces_aos(p, 1e-4)
+        f = O.ieee().forces_aos(p, 1e-4)
         O.ieee().integrate(p, v, f, 0.01, 0.95)
         g, _ = sysm.get_state()
         rel = _rel_pos(g, p)
