@@ -83,6 +83,25 @@ NBGB_API int nbgb_force_plan(size_t N, int config, int nsplit, int *out_config, 
 NBGB_API int nbgb_force_num_configs(void);
 NBGB_API const char *nbgb_force_config_name(int config);
 
+/*
+ * Allocation-free force evaluation.  No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc at run time -- hosts that own all
+ * device memory through their own pool or a budget fixed at start-up, and
+ * latency-critical step loops, where cudaMalloc/cudaFree may synchronise the
+ * device and take driver-wide locks.  Same sum and arguments as nbgb_force,
+ * but the scratch space is a fixed 32 MiB device array inside the library
+ * (held on every GPU that loads the library until the process exits), so
+ * nothing is allocated.  N is limited to 2,097,152 bodies; larger N returns
+ * NBGB_ERR_TOO_LARGE without launching anything.  All calls on a device share
+ * the array: calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's address (once per device); make it before capturing
+ * any stream.  Asynchronous on `stream`; returns NBGB_OK or NBGB_ERR_*.
+ */
+NBGB_API int nbgb_force_static(float *force, const float *posMass, float softeningSquared,
+                               size_t N, void *stream);
+/* Size of that fixed scratch array in bytes. */
+NBGB_API size_t nbgb_force_static_capacity_bytes(void);
+
 /* ======================================================================== */
 /* Integration step                                                          */
 /* ======================================================================== */

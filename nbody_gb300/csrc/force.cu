@@ -443,6 +443,50 @@ int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
     return NBGB_OK;
 }
 
+// The best plan (same cost model as plan_force) whose workspace fits in
+// max_bytes; NBGB_ERR_TOO_LARGE when none does.  Used by the fixed-scratch
+// entry point.
+int plan_force_within(size_t n, size_t max_bytes, ForcePlan &pl) {
+    if (n == 0 || n > kMaxBodies)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const DeviceInfo *d = device_info();
+    if (!d)
+        return NBGB_ERR_CUDA;
+    double best = 1e300;
+    bool found = false;
+    for (int c : kDefaultCandidates) {
+        const ForceConfig &cf = kConfigs[c];
+        const int occ = d->occ[c];
+        if (occ <= 0)
+            continue;
+        const double slots = (double)d->sms * occ;
+        const long long bi = (long long)cf.warps * 32 * cf.k;
+        const long long nb = ((long long)n + bi - 1) / bi;
+        const long long ntl = ((long long)n + cf.jt - 1) / cf.jt;
+        for (int s = 1; s <= (int)std::min<long long>(ntl, 256); s++) {
+            const long long units = nb * s;
+            if (units > (1ll << 31) - 1)
+                continue;
+            ForcePlan cand;
+            cand.config = c;
+            cand.nsplit = s;
+            fill_layout(cand, n);
+            if (cand.workspace_bytes > max_bytes)
+                continue;
+            const double waves = std::ceil((double)units / slots);
+            const double tiles = std::ceil((double)ntl / s);
+            const double t = waves * (tiles * cf.jt + 64.0 + (s > 1 ? 32.0 * s : 0.0)) *
+                             (double)bi * occ;
+            if (t < best * (1.0 - 1e-9)) {
+                best = t;
+                pl = cand;
+                found = true;
+            }
+        }
+    }
+    return found ? NBGB_OK : NBGB_ERR_TOO_LARGE;
+}
+
 int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,
                  float eps2, void *workspace, cudaStream_t stream) {
     const ForceConfig &cf = kConfigs[pl.config];

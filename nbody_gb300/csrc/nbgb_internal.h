@@ -26,6 +26,7 @@ struct ForcePlan {
 };
 
 int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl);
+int plan_force_within(size_t n, size_t max_bytes, ForcePlan &pl);
 int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream);
 // jstream == nullptr: use the j-stream inside the workspace.
 int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,
