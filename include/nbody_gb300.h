@@ -150,6 +150,11 @@ NBGB_API int nbgb_system_get_state(nbgb_system *sys, float *posMass, float *velI
 NBGB_API int nbgb_system_get_state64(nbgb_system *sys, double *pos3, double *vel3);
 /* Forces of the most recent force pass, HOST float4; synchronises. */
 NBGB_API int nbgb_system_get_force(nbgb_system *sys, float *force);
+/* Conserved quantities at the current state in FP64: out[0] kinetic,
+   out[1] potential energy (softened, self pairs excluded), out[2..4] linear
+   and out[5..7] angular momentum.  Costs one extra all-pairs pass (force
+   kernel with the potential); synchronises. */
+NBGB_API int nbgb_system_diagnostics(nbgb_system *sys, double *out);
 NBGB_API void *nbgb_system_device_posmass(nbgb_system *sys);
 NBGB_API void *nbgb_system_device_force(nbgb_system *sys);
 NBGB_API void *nbgb_system_stream(nbgb_system *sys);
@@ -176,6 +181,13 @@ NBGB_API int nbgb_ic_plummer(double *pos3, double *vel3, float *posMass, float *
 /* Replaces: the crosscheck loop (src/nbody.cu:120-125, 406-418): max over
    bodies and x,y,z of |a - b| / b (signed b).  HOST float4. */
 NBGB_API float nbgb_crosscheck_max_rel_error(const float *force, const float *golden, size_t N);
+/* FP64 all-pairs force (double[n_targets][3]) and potential (self pair
+   excluded; phi may be NULL) of the listed targets of a HOST float4 posMass,
+   on the host's threads: the library's FP64 yardstick for its FP32 results.
+   Pass eps2 as the binary32 value the GPU used. */
+NBGB_API int nbgb_force_f64_host(const float *posMass, size_t N, double eps2,
+                                 const long long *idx, size_t n_targets, double *force3,
+                                 double *phi);
 /* Per-body |F - T| / |T| against FP64 truth double[n_rows][3]; row t is body
    idx[t] (idx NULL: body t).  Max and RMS over rows. */
 NBGB_API int nbgb_force_error_stats(const float *force, const double *truth3,
@@ -189,7 +201,9 @@ NBGB_API int nbgb_force_error_stats(const float *force, const double *truth3,
 /* which: 0 = scalar FP32 FMA (FLOP/s, FMA = 2), 1 = packed f32x2 FMA
    (FLOP/s), 2 = MUFU rsqrt (results/s), 3 = packed add, 4 = packed multiply
    (FLOP/s, 2 per instruction), 5 = packed FMA with three varying register
-   operands.  Full-GPU launch of `iters` x 128 operations per thread, best of
+   operands, 6 = packed FMA with one MUFU rsqrt per six (FLOP/s of the
+   FMAs), 7 = packed and scalar FMA interleaved, 8 = the force kernel's
+   pair interaction on register-resident sources (20 FLOP/interaction).  Full-GPU launch of `iters` x 128 operations per thread, best of
    `reps` after a warm-up.  Synchronous. */
 NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms);
 

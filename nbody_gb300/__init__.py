@@ -145,7 +145,8 @@ def integrate_reference(posMass, velInvMass, force_, dt: float, damping: float, 
 def measure_peak(which: str, iters: int = 4096, reps: int = 5):
     """Measured pipe throughput: 'ffma' / 'ffma2' / 'fadd2' / 'fmul2' /
     'ffma2_3op' (FLOP/s) or 'mufu' (rsqrt/s)."""
-    code = {"ffma": 0, "ffma2": 1, "mufu": 2, "fadd2": 3, "fmul2": 4, "ffma2_3op": 5}[which]
+    code = {"ffma": 0, "ffma2": 1, "mufu": 2, "fadd2": 3, "fmul2": 4, "ffma2_3op": 5,
+            "ffma2_mufu": 6, "ffma2_ffma": 7, "interact": 8}[which]
     rate, ms = ctypes.c_double(), ctypes.c_float()
     check(load().nbgb_measure_peak(code, iters, reps, ctypes.byref(rate), ctypes.byref(ms)),
           "nbgb_measure_peak")
@@ -230,6 +231,13 @@ class System:
         check(self.lib.nbgb_system_get_force(self.h, _f32p(f)), "get_force")
         return f
 
+    def diagnostics(self) -> dict:
+        """FP64 kinetic/potential/total energy, momentum, angular momentum."""
+        out = np.zeros(8, np.float64)
+        check(self.lib.nbgb_system_diagnostics(self.h, _f64p(out)), "diagnostics")
+        return {"kinetic": out[0], "potential": out[1], "energy": out[0] + out[1],
+                "momentum": out[2:5].copy(), "angular_momentum": out[5:8].copy()}
+
     def plan(self):
         c, s = ctypes.c_int(), ctypes.c_int()
         check(self.lib.nbgb_system_plan(self.h, ctypes.byref(c), ctypes.byref(s)), "plan")
@@ -272,6 +280,18 @@ def ic_plummer(N: int, seed: int):
     check(load().nbgb_ic_plummer(_f64p(p), _f64p(v), _f32p(pm), _f32p(vm), N, seed),
           "ic_plummer")
     return p, v, pm, vm
+
+
+def force_f64_host(posMass: np.ndarray, softeningSquared: float, idx) -> tuple:
+    """FP64 force (n,3) and potential (n,) of targets idx (host threads)."""
+    pm = np.ascontiguousarray(posMass, np.float32)
+    idx = np.ascontiguousarray(idx, np.int64)
+    f = np.zeros((idx.shape[0], 3), np.float64)
+    phi = np.zeros(idx.shape[0], np.float64)
+    check(load().nbgb_force_f64_host(_f32p(pm), pm.shape[0], float(np.float32(softeningSquared)),
+                                     idx.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                     idx.shape[0], _f64p(f), _f64p(phi)), "force_f64_host")
+    return f, phi
 
 
 def crosscheck_max_rel_error(force_: np.ndarray, golden: np.ndarray) -> float:

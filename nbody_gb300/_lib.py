@@ -48,6 +48,7 @@ SIGNATURES = {
     "nbgb_system_get_state": (ctypes.c_int, [c_vp, c_f32p, c_f32p]),
     "nbgb_system_get_state64": (ctypes.c_int, [c_vp, c_f64p, c_f64p]),
     "nbgb_system_get_force": (ctypes.c_int, [c_vp, c_f32p]),
+    "nbgb_system_diagnostics": (ctypes.c_int, [c_vp, c_f64p]),
     "nbgb_system_device_posmass": (c_vp, [c_vp]),
     "nbgb_system_device_force": (c_vp, [c_vp]),
     "nbgb_system_stream": (c_vp, [c_vp]),
@@ -59,6 +60,8 @@ SIGNATURES = {
                                             ctypes.c_ulonglong]),
     "nbgb_ic_plummer": (ctypes.c_int, [c_f64p, c_f64p, c_f32p, c_f32p, c_size,
                                        ctypes.c_ulonglong]),
+    "nbgb_force_f64_host": (ctypes.c_int, [c_f32p, c_size, ctypes.c_double, c_i64p, c_size,
+                                           c_f64p, c_f64p]),
     "nbgb_crosscheck_max_rel_error": (ctypes.c_float, [c_f32p, c_f32p, c_size]),
     "nbgb_force_error_stats": (ctypes.c_int, [c_f32p, c_f64p, c_i64p, c_size, c_f64p, c_f64p]),
     "nbgb_measure_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_f64p,

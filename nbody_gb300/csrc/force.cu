@@ -79,6 +79,25 @@ __global__ void pack_jstream_kernel(const float4 *__restrict__ pm, float4 *__res
     js[2 * q + 1] = make_float4(b0.z, b1.z, b0.w, b1.w);
 }
 
+// pack, duplicated layout: body j -> {xj,xj,yj,yj},{zj,zj,mj,mj} (32 B), for
+// kernels that pair two targets per f32x2 register instead of two sources.
+__global__ void pack_jstream_dup_kernel(const float4 *__restrict__ pm, float4 *__restrict__ js,
+                                        int n, int npad, unsigned *__restrict__ counters,
+                                        int ncounters) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // pair of bodies
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int j = 2 * q + h;
+        if (j >= npad)
+            break;
+        const float4 b = (j < n) ? pm[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        js[2 * j] = make_float4(b.x, b.x, b.y, b.y);
+        js[2 * j + 1] = make_float4(b.z, b.z, b.w, b.w);
+    }
+    if (q < ncounters)
+        counters[q] = 0u;
+}
+
 // ---------------------------------------------------------------------------
 // force kernel
 // ---------------------------------------------------------------------------
@@ -86,8 +105,12 @@ template <int W, int K, int JT, int STAGES, int MODE, int UNROLL, int MINB>
 __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     constexpr int NT = W * 32;
     constexpr int BI = NT * K;
-    constexpr uint32_t TILE_BYTES = JT * 16u;
+    // float4s per source body in the j-stream: 1 (pairs of sources) or 2
+    // (MODE 4: each source duplicated, targets paired in registers)
+    constexpr int VPB = (MODE == 4) ? 2 : 1;
+    constexpr uint32_t TILE_BYTES = JT * 16u * VPB;
     static_assert(JT % 2 == 0, "tiles hold whole pairs");
+    static_assert(MODE != 4 || K % 2 == 0, "targets are paired");
 
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *ring = reinterpret_cast<float4 *>(smem_raw);
@@ -112,15 +135,19 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     if (tid == 0) {
         for (int s = 0; s < STAGES && s < nt; s++) {
             mbar_expect_tx(&full[s], TILE_BYTES);
-            bulk_g2s(ring + s * JT, p.jstream + (size_t)(t_begin + s) * JT, TILE_BYTES, &full[s]);
+            bulk_g2s(ring + s * JT * VPB, p.jstream + (size_t)(t_begin + s) * JT * VPB,
+                     TILE_BYTES, &full[s]);
             issued++;
         }
     }
 
     // Targets: thread tid owns bodies ib*BI + k*NT + tid (coalesced loads).
+    // MODE 5 also accumulates the potential sum_j m_j / r_ij (returned in w)
+    constexpr bool POT = (MODE == 5);
     f2 nx[K], ny[K], nz[K];     // packed mode: (-x,-x) etc.
     float px[K], py[K], pz[K];  // scalar mode
-    float hx[K], hy[K], hz[K], lx[K], ly[K], lz[K];
+    float pm_self[K];           // MODE 5: the target's own mass
+    float hx[K], hy[K], hz[K], lx[K], ly[K], lz[K], hp[K], lp[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
         const int i = ib * BI + k * NT + tid;
@@ -128,10 +155,20 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
         px[k] = b.x;
         py[k] = b.y;
         pz[k] = b.z;
+        pm_self[k] = b.w;
+        hp[k] = lp[k] = 0.f;
         nx[k] = f2_pack(-b.x, -b.x);
         ny[k] = f2_pack(-b.y, -b.y);
         nz[k] = f2_pack(-b.z, -b.z);
         hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
+    }
+    if constexpr (MODE == 4) {  // pair targets 2c and 2c+1 in one register pair
+#pragma unroll
+        for (int c = 0; c < K / 2; c++) {
+            nx[c] = f2_pack(-px[2 * c], -px[2 * c + 1]);
+            ny[c] = f2_pack(-py[2 * c], -py[2 * c + 1]);
+            nz[c] = f2_pack(-pz[2 * c], -pz[2 * c + 1]);
+        }
     }
     const f2 eps2p = f2_pack(p.eps2, p.eps2);
     const f2 zero2 = f2_pack(0.f, 0.f);
@@ -144,8 +181,62 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
         const uint32_t parity = (uint32_t)((t / STAGES) & 1);
         const bool ok = mbar_wait_bounded(&full[s], parity);
         if (ok) {
-            const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(ring + s * JT);
-            if (MODE != 0) {  // packed f32x2 (MODE 2: every op issued as an FMA)
+            const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(ring + s * JT * VPB);
+            if constexpr (MODE == 4) {  // targets paired, sources duplicated
+                constexpr int KP = K / 2 > 0 ? K / 2 : 1;
+                f2 ax[KP], ay[KP], az[KP];
+#pragma unroll
+                for (int c = 0; c < K / 2; c++)
+                    ax[c] = ay[c] = az[c] = zero2;
+#pragma unroll UNROLL
+                for (int j = 0; j < JT; j++) {
+                    const ulonglong2 a = tp[2 * j];      // (x,x) (y,y)
+                    const ulonglong2 b = tp[2 * j + 1];  // (z,z) (m,m)
+#pragma unroll
+                    for (int c = 0; c < K / 2; c++)
+                        pair_interact2(a.x, a.y, b.x, b.y, nx[c], ny[c], nz[c], eps2p, ax[c],
+                                       ay[c], az[c]);
+                }
+#pragma unroll
+                for (int c = 0; c < K / 2; c++) {
+                    float l, h;
+                    f2_unpack(ax[c], l, h);
+                    comp_add(hx[2 * c], lx[2 * c], l);
+                    comp_add(hx[2 * c + 1], lx[2 * c + 1], h);
+                    f2_unpack(ay[c], l, h);
+                    comp_add(hy[2 * c], ly[2 * c], l);
+                    comp_add(hy[2 * c + 1], ly[2 * c + 1], h);
+                    f2_unpack(az[c], l, h);
+                    comp_add(hz[2 * c], lz[2 * c], l);
+                    comp_add(hz[2 * c + 1], lz[2 * c + 1], h);
+                }
+            } else if constexpr (POT) {  // packed f32x2 with the potential
+                f2 ax[K], ay[K], az[K], ap[K];
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    ax[k] = ay[k] = az[k] = ap[k] = zero2;
+#pragma unroll UNROLL
+                for (int q = 0; q < JT / 2; q++) {
+                    const ulonglong2 a = tp[2 * q];
+                    const ulonglong2 b = tp[2 * q + 1];
+#pragma unroll
+                    for (int k = 0; k < K; k++)
+                        pair_interact2_pot(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p, ax[k],
+                                           ay[k], az[k], ap[k]);
+                }
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    float l, h;
+                    f2_unpack(ax[k], l, h);
+                    comp_add(hx[k], lx[k], l + h);
+                    f2_unpack(ay[k], l, h);
+                    comp_add(hy[k], ly[k], l + h);
+                    f2_unpack(az[k], l, h);
+                    comp_add(hz[k], lz[k], l + h);
+                    f2_unpack(ap[k], l, h);
+                    comp_add(hp[k], lp[k], l + h);
+                }
+            } else if constexpr (MODE != 0) {  // packed f32x2 (MODE 2: all ops as FMAs)
                 f2 ax[K], ay[K], az[K];
 #pragma unroll
                 for (int k = 0; k < K; k++)
@@ -207,8 +298,8 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
             break;
         if (tid == 0 && t + STAGES < nt) {
             mbar_expect_tx(&full[s], TILE_BYTES);
-            bulk_g2s(ring + s * JT, p.jstream + (size_t)(t_begin + t + STAGES) * JT, TILE_BYTES,
-                     &full[s]);
+            bulk_g2s(ring + s * JT * VPB, p.jstream + (size_t)(t_begin + t + STAGES) * JT * VPB,
+                     TILE_BYTES, &full[s]);
             issued++;
         }
     }
@@ -223,12 +314,20 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
         return;
     }
 
+    // MODE 5: w = -(sum_{j != i} m_j / r_ij); the self term the loop added is
+    // m_i * rsqrt(eps2), evaluated exactly as in the loop.
+    float self[K];
+#pragma unroll
+    for (int k = 0; k < K; k++)
+        self[k] = POT ? pm_self[k] * rsqrt_mufu(p.eps2) : 0.f;
+
     if (p.nsplit == 1) {
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const int i = ib * BI + k * NT + tid;
             if (i < p.n)
-                p.force[i] = make_float4(hx[k] + lx[k], hy[k] + ly[k], hz[k] + lz[k], 0.f);
+                p.force[i] = make_float4(hx[k] + lx[k], hy[k] + ly[k], hz[k] + lz[k],
+                                         POT ? -((hp[k] - self[k]) + lp[k]) : 0.f);
         }
         return;
     }
@@ -237,8 +336,8 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
 #pragma unroll
     for (int k = 0; k < K; k++) {
         const size_t o = (size_t)r * p.ni_pad + (size_t)(ib * BI + k * NT + tid);
-        p.part_hi[o] = make_float4(hx[k], hy[k], hz[k], 0.f);
-        p.part_lo[o] = make_float4(lx[k], ly[k], lz[k], 0.f);
+        p.part_hi[o] = make_float4(hx[k], hy[k], hz[k], hp[k]);
+        p.part_lo[o] = make_float4(lx[k], ly[k], lz[k], lp[k]);
     }
     __threadfence();
     __syncthreads();
@@ -257,12 +356,12 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
         const int i = ib * BI + k * NT + tid;
         if (i >= p.n)
             continue;
-        float Hx = 0.f, Hy = 0.f, Hz = 0.f, Lx = 0.f, Ly = 0.f, Lz = 0.f;
+        float Hx = 0.f, Hy = 0.f, Hz = 0.f, Lx = 0.f, Ly = 0.f, Lz = 0.f, Hp = 0.f, Lp = 0.f;
         for (int rr = 0; rr < p.nsplit; rr++) {
             float4 h, l;
             if (rr == r) {
-                h = make_float4(hx[k], hy[k], hz[k], 0.f);
-                l = make_float4(lx[k], ly[k], lz[k], 0.f);
+                h = make_float4(hx[k], hy[k], hz[k], hp[k]);
+                l = make_float4(lx[k], ly[k], lz[k], lp[k]);
             } else {
                 const size_t o = (size_t)rr * p.ni_pad + (size_t)i;
                 h = __ldcg(p.part_hi + o);
@@ -274,8 +373,12 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
             Lx += l.x;
             Ly += l.y;
             Lz += l.z;
+            if (POT) {
+                comp_add(Hp, Lp, h.w);
+                Lp += l.w;
+            }
         }
-        p.force[i] = make_float4(Hx + Lx, Hy + Ly, Hz + Lz, 0.f);
+        p.force[i] = make_float4(Hx + Lx, Hy + Ly, Hz + Lz, POT ? -((Hp - self[k]) + Lp) : 0.f);
     }
 }
 
@@ -284,14 +387,16 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
 // ---------------------------------------------------------------------------
 struct ForceConfig {
     int warps, k, jt, stages;
-    int mode;  // 0 scalar FP32, 1 packed f32x2, 2 packed with every op as an FMA
+    int mode;  // 0 scalar FP32, 1 packed f32x2 (source pairs), 2 as 1 with every
+               // op as an FMA, 4 packed f32x2 (target pairs, duplicated sources),
+               // 5 as 1 plus the potential in w
     const void *fn;
     const char *name;
 };
 
 // W warps, K targets per thread, JT sources per tile, ST ring stages, mode
-// (0 scalar, 1 f32x2, 2 f32x2 all-FMA), inner unroll, minimum resident CTAs
-// (register cap).
+// (0 scalar, 1 f32x2, 2 f32x2 all-FMA, 4 f32x2 target pairs, 5 f32x2 with
+// potential), inner unroll, minimum resident CTAs (register cap).
 #define NBGB_CFG(W, K, JT, ST, PK, UN, MB, PIPE)                                           \
     {W, K, JT, ST, PK, (const void *)force_kernel<W, K, JT, ST, PK, UN, MB>,               \
      "w" #W "_k" #K "_jt" #JT "_s" #ST "_" PIPE}
@@ -315,6 +420,12 @@ static const ForceConfig kConfigs[] = {
     NBGB_CFG(4, 8, 512, 3, 2, 2, 2, "fma2"),   // 15: as 5, all-FMA
     NBGB_CFG(8, 2, 256, 4, 2, 8, 2, "fma2"),   // 16: as 2, all-FMA
     NBGB_CFG(16, 2, 256, 4, 2, 4, 1, "fma2"),  // 17: as 9, all-FMA, unroll 4
+    NBGB_CFG(8, 4, 256, 4, 4, 4, 2, "tpair"),  // 18: target pairs, K 4
+    NBGB_CFG(8, 2, 256, 4, 4, 8, 3, "tpair"),  // 19: target pairs, K 2, 3 CTAs/SM
+    NBGB_CFG(8, 4, 256, 4, 4, 8, 2, "tpair"),  // 20: target pairs, K 4, unroll 8
+    NBGB_CFG(8, 6, 256, 4, 4, 4, 2, "tpair"),  // 21: target pairs, K 6
+    NBGB_CFG(4, 4, 256, 4, 4, 4, 4, "tpair"),  // 22: target pairs, K 4, 128 threads
+    NBGB_CFG(8, 2, 256, 4, 5, 4, 2, "pot"),    // 23: force + potential (diagnostics)
 };
 static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
 static const int kDefaultCandidates[] = {0, 1, 2, 3, 5};
@@ -348,7 +459,7 @@ static const DeviceInfo *device_info() {
     d.sms = prop.multiProcessorCount;
     for (int c = 0; c < kNumConfigs; c++) {
         const ForceConfig &cf = kConfigs[c];
-        const size_t smem = (size_t)cf.stages * cf.jt * 16;
+        const size_t smem = (size_t)cf.stages * cf.jt * 16 * (cf.mode == 4 ? 2 : 1);
         if (cudaFuncSetAttribute(cf.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
             return nullptr;
@@ -368,11 +479,12 @@ static void fill_layout(ForcePlan &pl, size_t n) {
     pl.n = n;
     pl.block_bodies = (int)bi;
     pl.tile_bodies = cf.jt;
+    pl.js_vpb = cf.mode == 4 ? 2 : 1;
     pl.nblocks = (int)((n + bi - 1) / bi);
     pl.ntiles = (int)((n + cf.jt - 1) / cf.jt);
     pl.ni_pad = (size_t)pl.nblocks * bi;
     pl.off_js = 0;
-    size_t o = align_up((size_t)pl.ntiles * cf.jt * 16, 256);
+    size_t o = align_up((size_t)pl.ntiles * cf.jt * 16 * pl.js_vpb, 256);
     if (pl.nsplit > 1) {
         pl.off_hi = o;
         o = align_up(o + (size_t)pl.nsplit * pl.ni_pad * 16, 256);
@@ -503,7 +615,7 @@ int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, cons
     p.nsplit = pl.nsplit;
     p.ni_pad = (int)pl.ni_pad;
     p.eps2 = eps2;
-    const size_t smem = (size_t)cf.stages * cf.jt * 16;
+    const size_t smem = (size_t)cf.stages * cf.jt * 16 * pl.js_vpb;
     void *args[] = {&p};
     const unsigned grid = (unsigned)((long long)pl.nblocks * pl.nsplit);
     cudaError_t e = cudaLaunchKernel(cf.fn, dim3(grid), dim3(cf.warps * 32), args, smem, stream);
@@ -518,8 +630,12 @@ int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cud
     const int ncnt = pl.nsplit > 1 ? pl.nblocks : 0;
     const int work = std::max(npad / 2, ncnt);
     const int tb = 256;
-    pack_jstream_kernel<<<(work + tb - 1) / tb, tb, 0, stream>>>(posMass, js, (int)pl.n, npad, cnt,
-                                                                  ncnt);
+    if (pl.js_vpb == 2)
+        pack_jstream_dup_kernel<<<(work + tb - 1) / tb, tb, 0, stream>>>(posMass, js, (int)pl.n,
+                                                                          npad, cnt, ncnt);
+    else
+        pack_jstream_kernel<<<(work + tb - 1) / tb, tb, 0, stream>>>(posMass, js, (int)pl.n, npad,
+                                                                      cnt, ncnt);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 

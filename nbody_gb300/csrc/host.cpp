@@ -17,9 +17,12 @@
 // All generators are deterministic in (seed, N) and portable: a splitmix64
 // stream, binary64 arithmetic with no contraction-sensitive expressions that
 // matter for equality tests, results rounded to binary32 at the end.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "nbody_gb300.h"
@@ -195,6 +198,60 @@ NBGB_API int nbgb_ic_plummer(double *pos3, double *vel3, float *posMass, float *
         if (velInvMass)
             velInvMass[4 * i + 3] = (float)(1.0 / m);
     }
+    return NBGB_OK;
+}
+
+// FP64 all-pairs force (and potential, self pair excluded) on the host for
+// the listed target bodies against all N sources -- the library's accuracy
+// yardstick for its own FP32 results (the reference's analogue is its CPU
+// crosscheck golden, src/nbody.cu:313-325).  Sources are the FP32 bodies
+// widened exactly; eps2 should be the binary32 value the GPU used.  Spread
+// over the host's hardware threads.  force3: double[n_targets][3]; phi may
+// be NULL.
+NBGB_API int nbgb_force_f64_host(const float *posMass, size_t N, double eps2,
+                                 const long long *idx, size_t n_targets, double *force3,
+                                 double *phi) {
+    if (!posMass || !force3 || (n_targets && !idx))
+        return NBGB_ERR_INVALID_ARGUMENT;
+    for (size_t t = 0; t < n_targets; t++)
+        if (idx[t] < 0 || (size_t)idx[t] >= N)
+            return NBGB_ERR_INVALID_ARGUMENT;
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (;;) {
+            const size_t t = next.fetch_add(1);
+            if (t >= n_targets)
+                return;
+            const size_t i = (size_t)idx[t];
+            const double x0 = posMass[4 * i], y0 = posMass[4 * i + 1], z0 = posMass[4 * i + 2];
+            double ax = 0, ay = 0, az = 0, p = 0;
+            for (size_t j = 0; j < N; j++) {
+                const double dx = (double)posMass[4 * j] - x0;
+                const double dy = (double)posMass[4 * j + 1] - y0;
+                const double dz = (double)posMass[4 * j + 2] - z0;
+                const double m = posMass[4 * j + 3];
+                const double inv = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz + eps2);
+                const double s = m * inv * inv * inv;
+                ax += dx * s;
+                ay += dy * s;
+                az += dz * s;
+                if (j != i)
+                    p -= m * inv;
+            }
+            force3[3 * t] = ax;
+            force3[3 * t + 1] = ay;
+            force3[3 * t + 2] = az;
+            if (phi)
+                phi[t] = p;
+        }
+    };
+    const unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), 256u));
+    std::vector<std::thread> pool;
+    for (unsigned k = 1; k < nt; k++)
+        pool.emplace_back(work);
+    work();
+    for (auto &th : pool)
+        th.join();
     return NBGB_OK;
 }
 

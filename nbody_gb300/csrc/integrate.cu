@@ -28,10 +28,25 @@
 namespace nbgb {
 
 // Thread q owns bodies 2q and 2q+1 (one j-stream pair).
+// j-stream store for bodies 2q, 2q+1 in either layout (vpb 1: source pairs,
+// vpb 2: each source duplicated).
+__device__ __forceinline__ void store_jstream(float4 *__restrict__ js, int vpb, int q, float4 b0,
+                                              float4 b1) {
+    if (vpb == 2) {
+        js[4 * q] = make_float4(b0.x, b0.x, b0.y, b0.y);
+        js[4 * q + 1] = make_float4(b0.z, b0.z, b0.w, b0.w);
+        js[4 * q + 2] = make_float4(b1.x, b1.x, b1.y, b1.y);
+        js[4 * q + 3] = make_float4(b1.z, b1.z, b1.w, b1.w);
+    } else {
+        js[2 * q] = make_float4(b0.x, b1.x, b0.y, b1.y);
+        js[2 * q + 1] = make_float4(b0.z, b1.z, b0.w, b1.w);
+    }
+}
+
 __global__ void integrate_reference_kernel(float4 *__restrict__ pm, float4 *__restrict__ vel,
                                            const float4 *__restrict__ force, float dt,
                                            float damping, int n, float4 *__restrict__ js,
-                                           int npad, unsigned *__restrict__ counters,
+                                           int js_vpb, int npad, unsigned *__restrict__ counters,
                                            int ncounters) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < ncounters)
@@ -58,10 +73,8 @@ __global__ void integrate_reference_kernel(float4 *__restrict__ pm, float4 *__re
             out[h] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
-    if (js && 2 * q < npad) {
-        js[2 * q] = make_float4(out[0].x, out[1].x, out[0].y, out[1].y);
-        js[2 * q + 1] = make_float4(out[0].z, out[1].z, out[0].w, out[1].w);
-    }
+    if (js && 2 * q < npad)
+        store_jstream(js, js_vpb, q, out[0], out[1]);
 }
 
 // FP64 kick (v += a * kick_dt) then drift (x += v * drift_dt); either may be
@@ -71,9 +84,8 @@ __global__ void kdk_kernel(double *__restrict__ px, double *__restrict__ py,
                            double *__restrict__ vy, double *__restrict__ vz,
                            const float *__restrict__ mass, const float4 *__restrict__ accel,
                            double kick_dt, double drift_dt, int write_pos, int n,
-                           float4 *__restrict__ pm,
-                           float4 *__restrict__ js, int npad, unsigned *__restrict__ counters,
-                           int ncounters) {
+                           float4 *__restrict__ pm, float4 *__restrict__ js, int js_vpb,
+                           int npad, unsigned *__restrict__ counters, int ncounters) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < ncounters)
         counters[q] = 0u;
@@ -108,33 +120,31 @@ __global__ void kdk_kernel(double *__restrict__ px, double *__restrict__ py,
             out[h] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
-    if (write_pos && js && 2 * q < npad) {
-        js[2 * q] = make_float4(out[0].x, out[1].x, out[0].y, out[1].y);
-        js[2 * q + 1] = make_float4(out[0].z, out[1].z, out[0].w, out[1].w);
-    }
+    if (write_pos && js && 2 * q < npad)
+        store_jstream(js, js_vpb, q, out[0], out[1]);
 }
 
 int launch_integrate_reference(float4 *pm, float4 *vel, const float4 *force, float dt,
-                               float damping, size_t n, float4 *js, int npad, unsigned *counters,
-                               int ncounters, cudaStream_t st) {
+                               float damping, size_t n, float4 *js, int js_vpb, int npad,
+                               unsigned *counters, int ncounters, cudaStream_t st) {
     const int pairs = (int)((n + 1) / 2);
     const int work = std::max(std::max(pairs, npad / 2), ncounters);
     const int tb = 256;
     integrate_reference_kernel<<<(work + tb - 1) / tb, tb, 0, st>>>(
-        pm, vel, force, dt, damping, (int)n, js, npad, counters, ncounters);
+        pm, vel, force, dt, damping, (int)n, js, js_vpb, npad, counters, ncounters);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
 int launch_kdk(double *px, double *py, double *pz, double *vx, double *vy, double *vz,
                const float *mass, const float4 *accel, double kick_dt, double drift_dt,
-               int write_pos, size_t n, float4 *pm, float4 *js, int npad, unsigned *counters,
-               int ncounters, cudaStream_t st) {
+               int write_pos, size_t n, float4 *pm, float4 *js, int js_vpb, int npad,
+               unsigned *counters, int ncounters, cudaStream_t st) {
     const int pairs = (int)((n + 1) / 2);
     const int work = std::max(std::max(pairs, npad / 2), ncounters);
     const int tb = 256;
     kdk_kernel<<<(work + tb - 1) / tb, tb, 0, st>>>(px, py, pz, vx, vy, vz, mass, accel, kick_dt,
-                                                    drift_dt, write_pos, (int)n, pm, js, npad,
-                                                    counters, ncounters);
+                                                    drift_dt, write_pos, (int)n, pm, js, js_vpb,
+                                                    npad, counters, ncounters);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
@@ -151,7 +161,7 @@ NBGB_API int nbgb_integrate_reference(float *posMass, float *velInvMass, const f
     if (((uintptr_t)posMass | (uintptr_t)velInvMass | (uintptr_t)force) & 15u)
         return NBGB_ERR_INVALID_ARGUMENT;
     return nbgb::launch_integrate_reference((float4 *)posMass, (float4 *)velInvMass,
-                                            (const float4 *)force, dt, damping, N, nullptr, 0,
+                                            (const float4 *)force, dt, damping, N, nullptr, 1, 0,
                                             nullptr, 0, (cudaStream_t)stream);
 }
 

@@ -99,6 +99,28 @@ __device__ __forceinline__ void pair_interact2(f2 sx, f2 sy, f2 sz, f2 sm,
     az = f2_fma(dz, s, az);
 }
 
+// pair_interact2 plus the potential sum ap += m * rsqrt(d2).
+__device__ __forceinline__ void pair_interact2_pot(f2 sx, f2 sy, f2 sz, f2 sm, f2 nx, f2 ny,
+                                                   f2 nz, f2 eps2, f2 &ax, f2 &ay, f2 &az,
+                                                   f2 &ap) {
+    f2 dx = f2_add(sx, nx);
+    f2 dy = f2_add(sy, ny);
+    f2 dz = f2_add(sz, nz);
+    f2 d2 = f2_fma(dx, dx, eps2);
+    d2 = f2_fma(dy, dy, d2);
+    d2 = f2_fma(dz, dz, d2);
+    float d2l, d2h;
+    f2_unpack(d2, d2l, d2h);
+    f2 inv = f2_pack(rsqrt_mufu(d2l), rsqrt_mufu(d2h));
+    f2 inv2 = f2_mul(inv, inv);
+    f2 s = f2_mul(sm, inv);
+    ap = f2_add(ap, s);
+    s = f2_mul(s, inv2);
+    ax = f2_fma(dx, s, ax);
+    ay = f2_fma(dy, s, ay);
+    az = f2_fma(dz, s, az);
+}
+
 // As pair_interact2, but every add and multiply is issued as an FMA
 // (a + b = fma(a, 1, b), a * b = fma(a, b, 0)); results are identical because
 // each FMA still rounds once.

@@ -20,6 +20,7 @@ struct ForcePlan {
     int tile_bodies = 0;  // sources per shared-memory tile (JT)
     int nblocks = 0;      // i-blocks
     int ntiles = 0;       // j-tiles (the j-stream holds ntiles*JT bodies)
+    int js_vpb = 1;       // float4s per body in the j-stream (1 pairs, 2 duplicated)
     size_t ni_pad = 0;    // nblocks * BI
     size_t off_js = 0, off_hi = 0, off_lo = 0, off_cnt = 0;
     size_t workspace_bytes = 0;
@@ -32,13 +33,20 @@ int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cud
 int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,
                  float eps2, void *workspace, cudaStream_t stream);
 int read_and_clear_status(unsigned *bits);
+// js_vpb: j-stream layout of the plan the j-stream is written for.
 int launch_integrate_reference(float4 *pm, float4 *vel, const float4 *force, float dt,
-                               float damping, size_t n, float4 *js, int npad, unsigned *counters,
-                               int ncounters, cudaStream_t st);
+                               float damping, size_t n, float4 *js, int js_vpb, int npad,
+                               unsigned *counters, int ncounters, cudaStream_t st);
 int launch_kdk(double *px, double *py, double *pz, double *vx, double *vy, double *vz,
                const float *mass, const float4 *accel, double kick_dt, double drift_dt,
-               int write_pos, size_t n, float4 *pm, float4 *js, int npad, unsigned *counters,
-               int ncounters, cudaStream_t st);
+               int write_pos, size_t n, float4 *pm, float4 *js, int js_vpb, int npad,
+               unsigned *counters, int ncounters, cudaStream_t st);
+size_t diag_scratch_bytes();
+int launch_diagnostics(int n, const double *x64, const float *mass, const float4 *pm,
+                       const float4 *vel, const float4 *phi, double *scratch, double *out8,
+                       cudaStream_t st);
+// force-kernel configuration that also returns the potential (in w)
+constexpr int kPotentialConfig = 23;
 const char *config_name(int c);
 int num_configs();
 

@@ -101,6 +101,94 @@ __global__ void __launch_bounds__(256) peak_f2op_kernel(float *out, int iters, f
         out[threadIdx.x] = s;
 }
 
+// Instruction mixes (which = 6, 7): about the force kernel's ratio of packed
+// FMAs to MUFU rsqrt (16 : 3 here, 6 : 1 there; FLOP/s of the FMAs), and
+// packed plus scalar FMAs issued together (FLOP/s of both).
+template <int MIX>
+__global__ void __launch_bounds__(256) peak_mix_kernel(float *out, int iters, float a, float b) {
+    f2 x[8], y[8];
+    float r[8];
+    const f2 aa = f2_pack(a, a), bb = f2_pack(b, b);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        x[c] = f2_pack((float)threadIdx.x, (float)c);
+        y[c] = f2_pack((float)c, (float)threadIdx.x);
+        r[c] = 1.0f + (float)(threadIdx.x + c);
+    }
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(x[c]) : "l"(aa), "l"(bb));
+                if (MIX == 6) {
+                    if (c % 3 == 0)
+                        asm volatile("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(r[c]));
+                } else {
+                    asm volatile("fma.rn.f32 %0, %0, %1, %2;" : "+f"(r[c]) : "f"(a), "f"(b));
+                }
+                asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(y[c]) : "l"(bb), "l"(aa));
+            }
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        float l, h, l2, h2;
+        f2_unpack(x[c], l, h);
+        f2_unpack(y[c], l2, h2);
+        s += l + h + l2 + h2 + r[c];
+    }
+    if (s == 1234.5f)
+        out[threadIdx.x] = s;
+}
+
+// The force kernel's pair interaction with sources in registers instead of
+// shared memory (which = 8): 2 targets x 4 source pairs per iteration;
+// reported as 20 FLOP per interaction, so it compares with the FP32 peak the
+// way the force kernel's figure does.
+__global__ void __launch_bounds__(256, 2) peak_interact_kernel(float *out, int iters, float a,
+                                                              float b) {
+    constexpr int KT = 2, NS = 4;
+    f2 nx[KT], ny[KT], nz[KT], ax[KT], ay[KT], az[KT];
+    f2 sx[NS], sy[NS], sz[NS], sm[NS];
+    const f2 eps2 = f2_pack(1e-4f, 1e-4f), step = f2_pack(a * 1e-7f, b * 1e-7f);
+#pragma unroll
+    for (int k = 0; k < KT; k++) {
+        const float t = (float)(threadIdx.x * KT + k) * 1e-3f;
+        nx[k] = f2_pack(-t, -t);
+        ny[k] = f2_pack(t, t);
+        nz[k] = f2_pack(0.5f * t, 0.5f * t);
+        ax[k] = ay[k] = az[k] = f2_pack(0.f, 0.f);
+    }
+#pragma unroll
+    for (int c = 0; c < NS; c++) {
+        sx[c] = f2_pack(0.1f * c, 0.1f * c + 0.05f);
+        sy[c] = f2_pack(-0.1f * c, 0.2f);
+        sz[c] = f2_pack(0.3f, 0.01f * c);
+        sm[c] = f2_pack(1e-3f, 2e-3f);
+    }
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int c = 0; c < NS; c++) {
+#pragma unroll
+            for (int k = 0; k < KT; k++)
+                pair_interact2(sx[c], sy[c], sz[c], sm[c], nx[k], ny[k], nz[k], eps2, ax[k],
+                               ay[k], az[k]);
+            sx[c] = f2_add(sx[c], step);
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < KT; k++) {
+        float l, h;
+        f2_unpack(f2_add(f2_add(ax[k], ay[k]), az[k]), l, h);
+        s += l + h;
+    }
+    if (s == 1234.5f)
+        out[threadIdx.x] = s;
+}
+
 __global__ void __launch_bounds__(256) peak_mufu_kernel(float *out, int iters) {
     float x[kChains];
 #pragma unroll
@@ -127,10 +215,13 @@ extern "C" {
 
 // which: 0 = FFMA (FLOP/s), 1 = FFMA2 (FLOP/s), 2 = MUFU rsqrt (ops/s),
 //        3 = add.f32x2, 4 = mul.f32x2 (FLOP/s, 2 per instruction), 5 = FFMA2
-//        with three varying operands (FLOP/s).
+//        with three varying operands (FLOP/s), 6 = FFMA2 with one MUFU rsqrt
+//        per six (FLOP/s of the FFMA2s), 7 = FFMA2 and scalar FFMA
+//        interleaved (FLOP/s of both), 8 = the force kernel's pair
+//        interaction on register-resident sources (20 FLOP/interaction).
 // Result in *rate; *ms = best launch time.  Synchronous.
 NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms_out) {
-    if (which < 0 || which > 5 || iters <= 0 || reps <= 0 || !rate)
+    if (which < 0 || which > 8 || iters <= 0 || reps <= 0 || !rate)
         return NBGB_ERR_INVALID_ARGUMENT;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -157,8 +248,14 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
             nbgb::peak_f2op_kernel<3><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
         else if (which == 4)
             nbgb::peak_f2op_kernel<4><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
-        else
+        else if (which == 5)
             nbgb::peak_f2op_kernel<5><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
+        else if (which == 6)
+            nbgb::peak_mix_kernel<6><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
+        else if (which == 7)
+            nbgb::peak_mix_kernel<7><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
+        else
+            nbgb::peak_interact_kernel<<<dim3(sms * 2), block>>>(out, iters / 8, 0.999f, 1e-3f);
         cudaEventRecord(e1, nullptr);
         if (cudaEventSynchronize(e1) != cudaSuccess)
             goto done;
@@ -177,6 +274,12 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
             ops *= 4.0;  // two FMAs per instruction
         else if (which == 3 || which == 4)
             ops *= 2.0;  // two adds / multiplies per instruction
+        else if (which == 6)
+            ops = threads * (double)iters * 8 * 8 * 2 * 4;  // FMAs of the FFMA2s only
+        else if (which == 7)
+            ops = threads * (double)iters * 8 * 8 * (2 * 4 + 2);  // FFMA2s + FFMAs
+        else if (which == 8)  // 20 FLOP x interactions: sms*2 CTAs, NS x KT x 2 per iteration
+            ops = (double)sms * 2 * block.x * (double)(iters / 8) * 4 * 2 * 2 * 20;
         *rate = ops / (best * 1e-3);
         if (ms_out)
             *ms_out = best;

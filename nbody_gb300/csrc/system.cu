@@ -47,6 +47,12 @@ struct nbgb_system {
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed_once = false;
+    // diagnostics (allocated on first use)
+    ForcePlan diag_plan;
+    void *diag_ws = nullptr;
+    float4 *phi = nullptr;
+    double *diag_scratch = nullptr;
+    double *diag_out = nullptr;
     int status = NBGB_OK;
 };
 
@@ -96,15 +102,16 @@ int ref_step_body(nbgb_system *s) {
     if (rc != NBGB_OK)
         return rc;
     return nbgb::launch_integrate_reference(s->pm, s->vel, s->force, s->dt, s->damping, s->n,
-                                            js_of(s), npad_of(s), cnt_of(s), ncnt_of(s),
-                                            s->stream);
+                                            js_of(s), s->plan.js_vpb, npad_of(s), cnt_of(s),
+                                            ncnt_of(s), s->stream);
 }
 
 // One fused leapfrog body: v += a*kick; x += v*dt; a = F(x).
 int kdk_body(nbgb_system *s, double kick) {
     int rc = nbgb::launch_kdk(comp(s, 0), comp(s, 1), comp(s, 2), comp(s, 3), comp(s, 4),
                               comp(s, 5), s->mass, s->force, kick, (double)s->dt, 1, s->n, s->pm,
-                              js_of(s), npad_of(s), cnt_of(s), ncnt_of(s), s->stream);
+                              js_of(s), s->plan.js_vpb, npad_of(s), cnt_of(s), ncnt_of(s),
+                              s->stream);
     if (rc != NBGB_OK)
         return rc;
     return timed_force(s);
@@ -112,8 +119,8 @@ int kdk_body(nbgb_system *s, double kick) {
 
 int half_kick(nbgb_system *s) {
     return nbgb::launch_kdk(comp(s, 0), comp(s, 1), comp(s, 2), comp(s, 3), comp(s, 4), comp(s, 5),
-                            s->mass, s->force, 0.5 * (double)s->dt, 0.0, 0, s->n, s->pm, nullptr, 0,
-                            nullptr, 0, s->stream);
+                            s->mass, s->force, 0.5 * (double)s->dt, 0.0, 0, s->n, s->pm, nullptr, 1,
+                            0, nullptr, 0, s->stream);
 }
 
 int check_device_status() {
@@ -136,6 +143,10 @@ void free_all(nbgb_system *s) {
     cudaFree(s->x64);
     cudaFree(s->mass);
     cudaFree(s->ws);
+    cudaFree(s->diag_ws);
+    cudaFree(s->phi);
+    cudaFree(s->diag_scratch);
+    cudaFree(s->diag_out);
     if (s->stream)
         cudaStreamDestroy(s->stream);
 }
@@ -416,6 +427,40 @@ NBGB_API int nbgb_system_get_force(nbgb_system *s, float *force) {
         return NBGB_ERR_INVALID_ARGUMENT;
     if (cudaMemcpyAsync(force, s->force, s->n * 16, cudaMemcpyDeviceToHost, s->stream) !=
             cudaSuccess ||
+        cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    return check_device_status();
+}
+
+// Conserved quantities at the current state, FP64: out[0] kinetic energy,
+// out[1] potential energy (softened, self pairs excluded), out[2..4] linear
+// momentum, out[5..7] angular momentum.  One force+potential pass (an extra
+// all-pairs evaluation) plus FP64 reductions; synchronises.
+NBGB_API int nbgb_system_diagnostics(nbgb_system *s, double *out) {
+    if (!s || !out)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const size_t n = s->n;
+    if (!s->diag_ws) {
+        int rc = nbgb::plan_force(n, nbgb::kPotentialConfig, -1, s->diag_plan);
+        if (rc != NBGB_OK)
+            return rc;
+        if (cudaMalloc(&s->diag_ws, s->diag_plan.workspace_bytes) != cudaSuccess ||
+            cudaMalloc(&s->phi, n * 16) != cudaSuccess ||
+            cudaMalloc(&s->diag_scratch, nbgb::diag_scratch_bytes()) != cudaSuccess ||
+            cudaMalloc(&s->diag_out, 8 * sizeof(double)) != cudaSuccess)
+            return NBGB_ERR_NO_MEMORY;
+    }
+    int rc = nbgb::launch_pack(s->diag_plan, s->pm, s->diag_ws, s->stream);
+    if (rc == NBGB_OK)
+        rc = nbgb::launch_force(s->diag_plan, s->phi, s->pm, nullptr, s->eps2, s->diag_ws,
+                                s->stream);
+    if (rc == NBGB_OK)
+        rc = nbgb::launch_diagnostics((int)n, s->x64, s->mass, s->pm, s->vel, s->phi,
+                                      s->diag_scratch, s->diag_out, s->stream);
+    if (rc != NBGB_OK)
+        return rc;
+    if (cudaMemcpyAsync(out, s->diag_out, 8 * sizeof(double), cudaMemcpyDeviceToHost,
+                        s->stream) != cudaSuccess ||
         cudaStreamSynchronize(s->stream) != cudaSuccess)
         return NBGB_ERR_CUDA;
     return check_device_status();
