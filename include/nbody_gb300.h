@@ -82,6 +82,11 @@ NBGB_API int nbgb_force_plan(size_t N, int config, int nsplit, int *out_config, 
                              size_t *out_workspace_bytes);
 NBGB_API int nbgb_force_num_configs(void);
 NBGB_API const char *nbgb_force_config_name(int config);
+/* Relative throughput the planner assumes for a configuration (measured
+   defaults); an autotuner sets measured values.  Not thread-safe against
+   concurrent planning. */
+NBGB_API int nbgb_force_set_speed(int config, double speed);
+NBGB_API double nbgb_force_get_speed(int config);
 
 /*
  * Allocation-free force evaluation.  No counterpart in the reference: it is

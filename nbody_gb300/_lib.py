@@ -31,6 +31,8 @@ SIGNATURES = {
                                        c_sizep]),
     "nbgb_force_num_configs": (ctypes.c_int, []),
     "nbgb_force_config_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "nbgb_force_set_speed": (ctypes.c_int, [ctypes.c_int, ctypes.c_double]),
+    "nbgb_force_get_speed": (ctypes.c_double, [ctypes.c_int]),
     "nbgb_force_static": (ctypes.c_int, [c_vp, c_vp, ctypes.c_float, c_size, c_vp]),
     "nbgb_force_static_capacity_bytes": (c_size, []),
     "nbgb_integrate_reference": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_float,

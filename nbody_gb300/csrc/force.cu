@@ -115,6 +115,9 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *ring = reinterpret_cast<float4 *>(smem_raw);
     __shared__ __align__(8) uint64_t full[STAGES];
+    __shared__ unsigned released[STAGES];  // warps that finished each stage, cumulative
+    __shared__ int stage_tile[STAGES];     // tile most recently issued into each stage
+    __shared__ int abort_flag;
     __shared__ int s_last;
 
     const int tid = threadIdx.x;
@@ -125,19 +128,23 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     const int t_end = (int)(((long long)(r + 1) * p.ntiles) / p.nsplit);
     const int nt = t_end - t_begin;
 
+    const int lane = tid & 31;
     if (tid == 0) {
-        for (int s = 0; s < STAGES; s++)
+        for (int s = 0; s < STAGES; s++) {
             mbar_init(&full[s], 1);
+            released[s] = 0u;
+            stage_tile[s] = -1;
+        }
+        abort_flag = 0;
         fence_mbar_init();
     }
     __syncthreads();
-    int issued = 0;  // tiles whose copy has been issued (meaningful in thread 0)
     if (tid == 0) {
         for (int s = 0; s < STAGES && s < nt; s++) {
             mbar_expect_tx(&full[s], TILE_BYTES);
             bulk_g2s(ring + s * JT * VPB, p.jstream + (size_t)(t_begin + s) * JT * VPB,
                      TILE_BYTES, &full[s]);
-            issued++;
+            stage_tile[s] = s;
         }
     }
 
@@ -174,13 +181,27 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     const f2 zero2 = f2_pack(0.f, 0.f);
     const f2 one2 = f2_pack(1.f, 1.f);
 
+    // Ring protocol without CTA-wide barriers: every warp waits for a stage's
+    // copy on its mbarrier, reads it, then releases it with an acq_rel add;
+    // the warp whose release completes the count for this round issues the
+    // copy of tile t + STAGES into the stage.  Waits are bounded; a warp
+    // whose wait runs out raises abort_flag and the others follow.
     bool failed = false;
-    int t = 0;
-    for (; t < nt; t++) {
+    for (int t = 0; t < nt; t++) {
         const int s = t % STAGES;
         const uint32_t parity = (uint32_t)((t / STAGES) & 1);
-        const bool ok = mbar_wait_bounded(&full[s], parity);
-        if (ok) {
+        if (__any_sync(0xffffffffu, *(volatile int *)&abort_flag != 0)) {
+            failed = true;
+            break;
+        }
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], parity));
+        if (!ok) {
+            if (lane == 0)
+                *(volatile int *)&abort_flag = 1;
+            failed = true;
+            break;
+        }
+        {
             const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(ring + s * JT * VPB);
             if constexpr (MODE == 4) {  // targets paired, sources duplicated
                 constexpr int KP = K / 2 > 0 ? K / 2 : 1;
@@ -291,26 +312,30 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                 }
             }
         }
-        // Every thread reaches this barrier (the waits are bounded), so a
-        // timeout anywhere makes the whole CTA leave together.
-        failed = __syncthreads_or(!ok) != 0;
-        if (failed)
-            break;
-        if (tid == 0 && t + STAGES < nt) {
-            mbar_expect_tx(&full[s], TILE_BYTES);
-            bulk_g2s(ring + s * JT * VPB, p.jstream + (size_t)(t_begin + t + STAGES) * JT * VPB,
-                     TILE_BYTES, &full[s]);
-            issued++;
+        __syncwarp();
+        if (lane == 0) {
+            const unsigned round = (unsigned)(t / STAGES) + 1u;
+            const unsigned prev = atom_add_acqrel_shared(&released[s], 1u);
+            if (prev == round * W - 1u && t + STAGES < nt) {
+                fence_proxy_async_shared();
+                mbar_expect_tx(&full[s], TILE_BYTES);
+                bulk_g2s(ring + s * JT * VPB,
+                         p.jstream + (size_t)(t_begin + t + STAGES) * JT * VPB, TILE_BYTES,
+                         &full[s]);
+                stage_tile[s] = t + STAGES;
+            }
         }
     }
-    if (failed) {
-        // Let copies still in flight (tiles t .. issued-1) land before the
-        // CTA's shared memory is released, again with a bounded wait, then
-        // leave without writing results.
+    // Every warp reaches this barrier (all waits are bounded).  After a
+    // timeout no warp issues copies any more; the last copy issued into each
+    // stage is waited for (bounded again) so no copy is still landing in
+    // shared memory when the CTA exits, and nothing is written.
+    if (__syncthreads_or(failed)) {
         if (tid == 0)
-            for (int u = t; u < issued; u++)
-                (void)mbar_wait_bounded(&full[u % STAGES], (uint32_t)((u / STAGES) & 1),
-                                        100000000ull);
+            for (int s = 0; s < STAGES; s++)
+                if (stage_tile[s] >= 0)
+                    (void)mbar_wait_bounded(&full[s], (uint32_t)((stage_tile[s] / STAGES) & 1),
+                                            100000000ull);
         return;
     }
 
@@ -426,9 +451,23 @@ static const ForceConfig kConfigs[] = {
     NBGB_CFG(8, 6, 256, 4, 4, 4, 2, "tpair"),  // 21: target pairs, K 6
     NBGB_CFG(4, 4, 256, 4, 4, 4, 4, "tpair"),  // 22: target pairs, K 4, 128 threads
     NBGB_CFG(8, 2, 256, 4, 5, 4, 2, "pot"),    // 23: force + potential (diagnostics)
+    NBGB_CFG(8, 2, 512, 3, 1, 4, 2, "f32x2"),  // 24: as 10, 512-body tiles
+    NBGB_CFG(8, 2, 1024, 2, 1, 4, 2, "f32x2"), // 25: as 10, 1024-body tiles
+    NBGB_CFG(8, 2, 128, 6, 1, 4, 2, "f32x2"),  // 26: as 10, 128-body tiles
 };
 static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
-static const int kDefaultCandidates[] = {0, 1, 2, 3, 5};
+// Relative throughput of each configuration (interactions/s per resident
+// CTA slot, normalised to configuration 25), measured on a GB300 at
+// N = 1,048,576 Plummer; the planner divides its wave cost by it.  An
+// autotuner can replace the values at run time (nbgb_force_set_speed).
+static double g_speed[] = {
+    0.943, 0.934, 0.981, 0.970, 0.902, 0.981, 0.955, 0.954, 0.962, 0.973,  // 0-9
+    0.990, 0.966, 0.873, 0.936, 0.987, 0.981, 0.981, 0.982, 0.981, 0.928,  // 10-19
+    0.987, 0.951, 0.974, 0.900, 0.997, 1.000, 0.977,                       // 20-26
+};
+static_assert(sizeof(g_speed) / sizeof(g_speed[0]) == sizeof(kConfigs) / sizeof(kConfigs[0]),
+              "one speed per configuration");
+static const int kDefaultCandidates[] = {25, 24, 10, 20, 2, 3, 5};
 
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -539,7 +578,7 @@ int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
             const double tiles = std::ceil((double)ntl / s);
             // + small per-unit overhead (prologue, partial write and combine)
             const double t = waves * (tiles * cf.jt + 64.0 + (s > 1 ? 32.0 * s : 0.0)) *
-                             (double)bi * occ;
+                             (double)bi * occ / g_speed[c];
             if (t < best * (1.0 - 1e-9)) {
                 best = t;
                 best_c = c;
@@ -588,7 +627,7 @@ int plan_force_within(size_t n, size_t max_bytes, ForcePlan &pl) {
             const double waves = std::ceil((double)units / slots);
             const double tiles = std::ceil((double)ntl / s);
             const double t = waves * (tiles * cf.jt + 64.0 + (s > 1 ? 32.0 * s : 0.0)) *
-                             (double)bi * occ;
+                             (double)bi * occ / g_speed[c];
             if (t < best * (1.0 - 1e-9)) {
                 best = t;
                 pl = cand;
@@ -726,6 +765,17 @@ NBGB_API int nbgb_force_plan(size_t N, int config, int nsplit, int *out_config, 
 }
 
 NBGB_API const char *nbgb_force_config_name(int config) { return config_name(config); }
+
+NBGB_API int nbgb_force_set_speed(int config, double speed) {
+    if (config < 0 || config >= kNumConfigs || !(speed > 0.0))
+        return NBGB_ERR_INVALID_ARGUMENT;
+    g_speed[config] = speed;
+    return NBGB_OK;
+}
+
+NBGB_API double nbgb_force_get_speed(int config) {
+    return (config >= 0 && config < kNumConfigs) ? g_speed[config] : 0.0;
+}
 NBGB_API int nbgb_force_num_configs(void) { return num_configs(); }
 
 NBGB_API int nbgb_force_ex(float *force, const float *posMass, float softeningSquared, size_t N,

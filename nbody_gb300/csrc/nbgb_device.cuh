@@ -220,6 +220,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return done != 0;
 }
 
+// Shared-memory add with acquire-release semantics at CTA scope: a warp that
+// finished reading a ring stage releases it; the warp that completes the
+// count acquires every other warp's reads before reusing the stage.
+__device__ __forceinline__ unsigned atom_add_acqrel_shared(unsigned *p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;"
+                 : "=r"(old)
+                 : "r"(smem_addr(p)), "r"(v)
+                 : "memory");
+    return old;
+}
+
+// Orders this thread's (acquired) generic-proxy shared-memory accesses before
+// its following async-proxy (bulk copy) accesses to shared memory.
+__device__ __forceinline__ void fence_proxy_async_shared() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 __device__ __forceinline__ uint64_t global_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));

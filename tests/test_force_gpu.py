@@ -58,7 +58,7 @@ def test_drop_in_entry_matches_reference(cuda, case):
     assert np.isfinite(nb.crosscheck_max_rel_error(out, g["force_aos"]))
 
 
-@pytest.mark.parametrize("config", range(23))
+@pytest.mark.parametrize("config", range(27))
 @pytest.mark.parametrize("nsplit", [1, 2, 3, 7])
 def test_every_configuration_and_split(cuda, config, nsplit):
     g = golden("plummer4096")
