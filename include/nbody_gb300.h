@@ -166,6 +166,50 @@ NBGB_API void *nbgb_system_stream(nbgb_system *sys);
 NBGB_API int nbgb_system_plan(nbgb_system *sys, int *config, int *nsplit);
 
 /* ======================================================================== */
+/* Ensembles of independent systems (batched and served)                     */
+/* ======================================================================== */
+
+/* No counterpart in the reference (it evaluates one system per call,
+   src/nbody.h:68).  All active systems live in one device arena; a tick
+   advances every one by an FP64 kick-drift-kick step with three launches, the
+   force pass being ONE persistent launch over a device queue of (system,
+   i-block, j-split) work items.  A system's plan depends only on its N, so
+   results are bit-identical alone or in any mix.  Host calls on one ensemble
+   must come from one thread. */
+typedef struct nbgb_ensemble nbgb_ensemble;
+
+/* Allocates the whole arena for max_bodies bodies / max_systems systems;
+   NULL on failure.  nbgb_ensemble_device_bytes reports its size. */
+NBGB_API nbgb_ensemble *nbgb_ensemble_create(size_t max_bodies, int max_systems,
+                                             float softeningSquared);
+NBGB_API void nbgb_ensemble_destroy(nbgb_ensemble *ens);
+NBGB_API size_t nbgb_ensemble_device_bytes(nbgb_ensemble *ens);
+/* Plan for N in [2^bucket, 2^(bucket+1)): variant 0..3 = (targets per
+   thread, unroll) (1,8) (2,4) (1,4) (2,8); tile 16..1024 bodies (multiple of
+   16); j-split 1..4; variant -1 = the default rule. */
+NBGB_API int nbgb_ensemble_set_bucket_plan(nbgb_ensemble *ens, int bucket, int variant, int jt,
+                                           int nsplit);
+/* Admit a system (HOST double[n][3] x, v; float m[n]); NBGB_ERR_NO_MEMORY if
+   no slot or arena space is free.  Its first tick computes its initial
+   accelerations; each later tick is one KDK step of size dt, `steps` times. */
+NBGB_API int nbgb_ensemble_add(nbgb_ensemble *ens, const double *pos3, const double *vel3,
+                               const float *mass, size_t n, double dt, long long steps,
+                               int *slot);
+NBGB_API int nbgb_ensemble_tick(nbgb_ensemble *ens, int nticks);
+NBGB_API int nbgb_ensemble_set_graph(nbgb_ensemble *ens, int enable);
+NBGB_API int nbgb_ensemble_synchronize(nbgb_ensemble *ens);
+/* Up to max slots whose steps are done; returns the count. */
+NBGB_API int nbgb_ensemble_finished(nbgb_ensemble *ens, int *slots, int max);
+/* HOST double[n][3] x, v and float4 accelerations (any may be NULL). */
+NBGB_API int nbgb_ensemble_get_state(nbgb_ensemble *ens, int slot, double *pos3, double *vel3,
+                                     float *acc4);
+/* info[6]: bodies, steps done, steps left, variant, tile, j-split. */
+NBGB_API int nbgb_ensemble_slot_info(nbgb_ensemble *ens, int slot, long long *info6);
+NBGB_API int nbgb_ensemble_remove(nbgb_ensemble *ens, int slot);
+NBGB_API int nbgb_ensemble_active(nbgb_ensemble *ens);
+NBGB_API void *nbgb_ensemble_stream(nbgb_ensemble *ens);
+
+/* ======================================================================== */
 /* Initial conditions and error statistics (host)                            */
 /* ======================================================================== */
 

@@ -248,6 +248,97 @@ class System:
         return int(self.lib.nbgb_system_stream(self.h) or 0)
 
 
+class Ensemble:
+    """Many independent systems resident in one device arena; tick() moves
+    all of them one FP64 KDK step with one persistent force launch."""
+
+    def __init__(self, max_bodies: int, max_systems: int, softeningSquared: float = 1e-4,
+                 tuning="auto"):
+        """tuning: "auto" applies the autotuner's table (nbody_gb300/tuning/
+        ensemble.json) when present, a dict applies that table, None keeps the
+        library's default per-bucket rule."""
+        self.lib = load()
+        self.h = self.lib.nbgb_ensemble_create(max_bodies, max_systems, softeningSquared)
+        if not self.h:
+            raise NbgbError(-6, "nbgb_ensemble_create")
+        self._n = {}
+        if tuning is not None:
+            from . import autotune
+            autotune.apply(self, autotune.load() if tuning == "auto" else tuning)
+
+    def close(self):
+        if self.h:
+            self.lib.nbgb_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.lib.nbgb_ensemble_device_bytes(self.h))
+
+    def set_bucket_plan(self, bucket: int, variant: int, jt: int = 256, nsplit: int = 1):
+        check(self.lib.nbgb_ensemble_set_bucket_plan(self.h, bucket, variant, jt, nsplit),
+              "set_bucket_plan")
+
+    def add(self, pos3, vel3, mass, dt: float, steps: int):
+        """Admit a system; returns its slot, or None when the arena is full."""
+        p = np.ascontiguousarray(pos3, np.float64)
+        v = np.ascontiguousarray(vel3, np.float64)
+        m = np.ascontiguousarray(mass, np.float32)
+        slot = ctypes.c_int(-1)
+        rc = self.lib.nbgb_ensemble_add(self.h, _f64p(p), _f64p(v), _f32p(m), p.shape[0], dt,
+                                        steps, ctypes.byref(slot))
+        if rc == -6:
+            return None
+        check(rc, "ensemble_add")
+        self._n[slot.value] = p.shape[0]
+        return slot.value
+
+    def tick(self, n: int = 1):
+        check(self.lib.nbgb_ensemble_tick(self.h, n), "ensemble_tick")
+
+    def use_graph(self, enable: bool):
+        check(self.lib.nbgb_ensemble_set_graph(self.h, int(enable)), "ensemble_set_graph")
+
+    def synchronize(self):
+        check(self.lib.nbgb_ensemble_synchronize(self.h), "ensemble_synchronize")
+
+    def finished(self, max_n: int = 65536):
+        buf = (ctypes.c_int * max_n)()
+        k = self.lib.nbgb_ensemble_finished(self.h, buf, max_n)
+        if k < 0:
+            check(k, "ensemble_finished")
+        return [buf[i] for i in range(k)]
+
+    def get_state(self, slot: int):
+        n = self._n[slot]
+        p = np.zeros((n, 3), np.float64)
+        v = np.zeros((n, 3), np.float64)
+        a = np.zeros((n, 4), np.float32)
+        check(self.lib.nbgb_ensemble_get_state(self.h, slot, _f64p(p), _f64p(v), _f32p(a)),
+              "ensemble_get_state")
+        return p, v, a
+
+    def slot_info(self, slot: int) -> dict:
+        info = np.zeros(6, np.int64)
+        check(self.lib.nbgb_ensemble_slot_info(
+            self.h, slot, info.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))), "slot_info")
+        return {"n": int(info[0]), "steps_done": int(info[1]), "steps_left": int(info[2]),
+                "variant": int(info[3]), "jt": int(info[4]), "nsplit": int(info[5])}
+
+    def remove(self, slot: int):
+        check(self.lib.nbgb_ensemble_remove(self.h, slot), "ensemble_remove")
+        self._n.pop(slot, None)
+
+    def active(self) -> int:
+        return int(self.lib.nbgb_ensemble_active(self.h))
+
+
 # ---------------------------------------------------------------------------
 # Initial conditions, metrics (host)
 # ---------------------------------------------------------------------------
@@ -312,6 +403,11 @@ def force_error_stats(force_: np.ndarray, truth3: np.ndarray, idx=None):
     check(load().nbgb_force_error_stats(_f32p(f), _f64p(t), ip, t.shape[0], ctypes.byref(mx),
                                         ctypes.byref(rms)), "force_error_stats")
     return mx.value, rms.value
+
+
+def bucket_of(n: int) -> int:
+    """Ensemble plan bucket of a system size: N in [2^b, 2^(b+1))."""
+    return max(0, int(n).bit_length() - 1)
 
 
 def interactions_per_second(N: int, ms: float) -> float:

@@ -55,6 +55,22 @@ SIGNATURES = {
     "nbgb_system_device_force": (c_vp, [c_vp]),
     "nbgb_system_stream": (c_vp, [c_vp]),
     "nbgb_system_plan": (ctypes.c_int, [c_vp, c_intp, c_intp]),
+    "nbgb_ensemble_create": (c_vp, [c_size, ctypes.c_int, ctypes.c_float]),
+    "nbgb_ensemble_destroy": (None, [c_vp]),
+    "nbgb_ensemble_device_bytes": (c_size, [c_vp]),
+    "nbgb_ensemble_set_bucket_plan": (ctypes.c_int, [c_vp, ctypes.c_int, ctypes.c_int,
+                                                     ctypes.c_int, ctypes.c_int]),
+    "nbgb_ensemble_add": (ctypes.c_int, [c_vp, c_f64p, c_f64p, c_f32p, c_size, ctypes.c_double,
+                                         ctypes.c_longlong, c_intp]),
+    "nbgb_ensemble_tick": (ctypes.c_int, [c_vp, ctypes.c_int]),
+    "nbgb_ensemble_set_graph": (ctypes.c_int, [c_vp, ctypes.c_int]),
+    "nbgb_ensemble_synchronize": (ctypes.c_int, [c_vp]),
+    "nbgb_ensemble_finished": (ctypes.c_int, [c_vp, c_intp, ctypes.c_int]),
+    "nbgb_ensemble_get_state": (ctypes.c_int, [c_vp, ctypes.c_int, c_f64p, c_f64p, c_f32p]),
+    "nbgb_ensemble_slot_info": (ctypes.c_int, [c_vp, ctypes.c_int, c_i64p]),
+    "nbgb_ensemble_remove": (ctypes.c_int, [c_vp, ctypes.c_int]),
+    "nbgb_ensemble_active": (ctypes.c_int, [c_vp]),
+    "nbgb_ensemble_stream": (c_vp, [c_vp]),
     "nbgb_ic_reference": (ctypes.c_int, [c_f32p, c_f32p, c_size, ctypes.c_float,
                                          ctypes.c_float, ctypes.c_uint]),
     "nbgb_ic_uniform_ball": (ctypes.c_int, [c_f32p, c_f32p, c_size, ctypes.c_double,

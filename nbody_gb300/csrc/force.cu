@@ -686,6 +686,8 @@ static NBGB_STATUS_READER(read_status_force)
 int read_and_clear_status(unsigned *bits) {
     *bits = 0;
     int rc = read_status_force(bits);
+    if (rc == NBGB_OK)
+        rc = read_status_ensemble(bits);
     return rc;
 }
 

@@ -33,6 +33,7 @@ int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cud
 int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,
                  float eps2, void *workspace, cudaStream_t stream);
 int read_and_clear_status(unsigned *bits);
+int read_status_ensemble(unsigned *bits);
 // js_vpb: j-stream layout of the plan the j-stream is written for.
 int launch_integrate_reference(float4 *pm, float4 *vel, const float4 *force, float dt,
                                float damping, size_t n, float4 *js, int js_vpb, int npad,

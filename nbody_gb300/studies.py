@@ -1,8 +1,12 @@
-"""Precision study: FP32 forces with compensated sums under an FP64
-kick-drift-kick integrator.
+"""Studies on the resident GB300 path: the precision study and the batched
+ensemble against looping the plain kernel.
 
     python -m nbody_gb300.studies precision [--n 262144] [--steps 1000]
         [--dt 0.002] [--eps2 1e-4] [--sample 4096] [--every 100] [--seed 262144]
+    python -m nbody_gb300.studies batched [--systems 4096] [--steps 100]
+        [--dt 0.01] [--eps2 1e-4] [--seed 4096] [--plain-sample 4096]
+
+Precision study:
 
 Seeded Plummer sphere (G = M = a = 1, equal masses), state resident on the
 GPU.  Reports the max and RMS per-body relative force error of the GPU's FP32
@@ -86,18 +90,114 @@ def precision_study(n: int = 262144, steps: int = 1000, dt: float = 0.002, eps2:
     }
 
 
+def ensemble_systems(n_systems: int, n_lo: int, n_hi: int, seed: int, mass_lo: float = 0.5,
+                     mass_hi: float = 1.5):
+    """Seeded systems: N log-uniform in [n_lo, n_hi], uniform ball of radius 1,
+    masses U[mass_lo, mass_hi] / N, zero velocities."""
+    from . import ic_uniform_ball
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), n_systems))
+    sizes = np.clip(np.rint(sizes).astype(int), n_lo, n_hi)
+    out = []
+    for k, n in enumerate(sizes):
+        pm, _ = ic_uniform_ball(int(n), seed * 100003 + k, 1.0, mass_lo, mass_hi)
+        p = pm[:, :3].astype(np.float64)
+        out.append((p, np.zeros_like(p), pm[:, 3].copy()))
+    return out
+
+
+def batched_study(n_systems: int = 4096, n_lo: int = 64, n_hi: int = 8192, steps: int = 100,
+                  dt: float = 0.01, eps2: float = 1e-4, seed: int = 4096,
+                  plain_sample: int = 4096) -> dict:
+    """Every system advanced `steps` FP64 KDK steps, once through the ensemble
+    (one persistent force launch per step for all systems, CUDA-graph ticks)
+    and once by looping the plain single-system path over the systems (one
+    System per system, eager launches).  The plain loop may run on a seeded
+    subsample of `plain_sample` systems; its systems/s then scales by the
+    sample's share of the interactions (stated in the result)."""
+    import torch
+
+    from . import INTEGRATOR_KDK64, Ensemble, System
+
+    systems = ensemble_systems(n_systems, n_lo, n_hi, seed)
+    sizes = np.array([p.shape[0] for p, _, _ in systems])
+    inter = float((sizes.astype(np.float64) ** 2).sum()) * (steps + 1)
+
+    e = Ensemble(int(sizes.sum()), n_systems, eps2)
+    t0 = time.perf_counter()
+    slots = [e.add(p, v, m, dt, steps) for p, v, m in systems]
+    admit_s = time.perf_counter() - t0
+    assert all(s is not None for s in slots)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e.tick(steps + 1)
+    e.synchronize()
+    ens_s = time.perf_counter() - t0
+    assert len(e.finished()) == n_systems
+    e.close()
+
+    # plain loop (sequential, one system at a time)
+    rng = np.random.default_rng(seed + 1)
+    pick = np.arange(n_systems) if plain_sample >= n_systems else np.sort(
+        rng.choice(n_systems, plain_sample, replace=False))
+    plain_s = 0.0
+    plain_inter = 0.0
+    for k in pick:
+        p, v, m = systems[k]
+        n = p.shape[0]
+        s = System(n, INTEGRATOR_KDK64, eps2, dt, 1.0)
+        s.use_graph(False)
+        s.set_state64(p, v, m)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.step(steps)
+        s.synchronize()
+        plain_s += time.perf_counter() - t0
+        plain_inter += float(n) * n * (steps + 1)
+        s.close()
+    plain_full_s = plain_s * inter / plain_inter
+    return {
+        "study": "batched",
+        "systems": n_systems, "n_range": [n_lo, n_hi], "steps": steps, "dt": dt,
+        "softeningSquared": eps2, "seed": seed, "total_bodies": int(sizes.sum()),
+        "interactions": inter,
+        "ensemble_seconds": ens_s, "ensemble_systems_per_s": n_systems / ens_s,
+        "ensemble_interactions_per_s": inter / ens_s,
+        "ensemble_admission_seconds": admit_s,
+        "plain_sample": int(len(pick)), "plain_seconds_sample": plain_s,
+        "plain_seconds_full_estimate": plain_full_s,
+        "plain_systems_per_s": n_systems / plain_full_s,
+        "plain_interactions_per_s": plain_inter / plain_s,
+        "speedup": plain_full_s / ens_s,
+    }
+
+
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision"])
-    ap.add_argument("--n", type=int, default=262144)
-    ap.add_argument("--steps", type=int, default=1000)
-    ap.add_argument("--dt", type=float, default=0.002)
-    ap.add_argument("--eps2", type=float, default=1e-4)
-    ap.add_argument("--sample", type=int, default=4096)
-    ap.add_argument("--every", type=int, default=100)
-    ap.add_argument("--seed", type=int, default=262144)
+    sub = ap.add_subparsers(dest="study", required=True)
+    pr = sub.add_parser("precision")
+    pr.add_argument("--n", type=int, default=262144)
+    pr.add_argument("--steps", type=int, default=1000)
+    pr.add_argument("--dt", type=float, default=0.002)
+    pr.add_argument("--eps2", type=float, default=1e-4)
+    pr.add_argument("--sample", type=int, default=4096)
+    pr.add_argument("--every", type=int, default=100)
+    pr.add_argument("--seed", type=int, default=262144)
+    ba = sub.add_parser("batched")
+    ba.add_argument("--systems", type=int, default=4096)
+    ba.add_argument("--n-lo", type=int, default=64)
+    ba.add_argument("--n-hi", type=int, default=8192)
+    ba.add_argument("--steps", type=int, default=100)
+    ba.add_argument("--dt", type=float, default=0.01)
+    ba.add_argument("--eps2", type=float, default=1e-4)
+    ba.add_argument("--seed", type=int, default=4096)
+    ba.add_argument("--plain-sample", type=int, default=4096)
     a = ap.parse_args(argv)
-    r = precision_study(a.n, a.steps, a.dt, a.eps2, a.seed, a.sample, a.every)
+    if a.study == "precision":
+        r = precision_study(a.n, a.steps, a.dt, a.eps2, a.seed, a.sample, a.every)
+    else:
+        r = batched_study(a.systems, a.n_lo, a.n_hi, a.steps, a.dt, a.eps2, a.seed,
+                          a.plain_sample)
     print(json.dumps(r))
 
 

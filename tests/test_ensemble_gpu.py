@@ -1,0 +1,146 @@
+"""Ensembles: one persistent force launch over many systems of uneven N.
+Forces against FP64, alone-vs-mixed bit identity (also when systems join and
+leave mid-run), admission limits, and agreement with the single-system path."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+import nbody_gb300 as nb
+
+pytestmark = pytest.mark.gpu
+
+TOL_VS_FP64 = 5e-6
+EPS2 = 1e-4
+
+
+def _ball(n, seed):
+    pm, _ = nb.ic_uniform_ball(n, seed, 1.0, 0.5, 1.5)
+    p = pm[:, :3].astype(np.float64)
+    v = np.zeros_like(p)
+    return p, v, pm[:, 3].copy(), pm
+
+
+def _f64(pm):
+    f = np.zeros((pm.shape[0], 4))
+    f[:, :3] = O.ieee().forces_f64(pm, float(np.float32(EPS2)))
+    return f
+
+
+@pytest.mark.parametrize("variant,jt,nsplit", [(0, 128, 1), (1, 256, 1), (1, 512, 3),
+                                               (0, 1024, 2), (1, 1024, 1), (-1, 256, 1)])
+def test_initial_forces_match_fp64(cuda, variant, jt, nsplit):
+    e = nb.Ensemble(60000, 16, EPS2)
+    for b in range(32):
+        e.set_bucket_plan(b, variant, jt, nsplit)
+    sizes = [1, 33, 64, 700, 1000, 2500, 5003, 8192]
+    slots, pms = [], []
+    for k, n in enumerate(sizes):
+        p, v, m, pm = _ball(n, 100 + k)
+        slots.append(e.add(p, v, m, 0.01, 5))
+        pms.append(pm)
+    e.tick(1)  # initial accelerations only
+    e.synchronize()
+    for s, pm in zip(slots, pms):
+        p1, v1, a = e.get_state(s)
+        assert np.array_equal(p1, pm[:, :3].astype(np.float64))  # nothing moved yet
+        if pm.shape[0] == 1:
+            assert np.all(a[0, :3] == 0)
+            continue
+        assert O.per_body_rel_error(a, _f64(pm))[0] <= TOL_VS_FP64
+    e.close()
+
+
+def test_alone_and_mixed_are_bit_identical_with_joins_and_leaves(cuda):
+    dt, steps = 0.002, 6
+    cases = {n: _ball(n, n) for n in (300, 1500, 4100, 7000)}
+
+    def run(members, join_at):
+        e = nb.Ensemble(40000, 8, EPS2)
+        slots, out, t = {}, {}, 0
+        pending = sorted(members, key=lambda n: join_at.get(n, 0))
+        while pending or slots:
+            for n in list(pending):
+                if join_at.get(n, 0) <= t:
+                    p, v, m, _ = cases[n]
+                    slots[n] = e.add(p, v, m, dt, steps)
+                    pending.remove(n)
+            e.tick(1)
+            t += 1
+            for s in e.finished():
+                n = next(k for k, v in slots.items() if v == s)
+                out[n] = e.get_state(s)
+                e.remove(s)
+                del slots[n]
+        e.close()
+        return out
+
+    alone = {n: run([n], {})[n] for n in cases}
+    mixed = run(list(cases), {300: 0, 1500: 2, 4100: 3, 7000: 9})
+    for n in cases:
+        for a, b in zip(alone[n], mixed[n]):
+            assert np.array_equal(a, b), n
+
+
+def test_matches_single_system_kdk(cuda):
+    n, dt, steps = 3000, 0.002, 20
+    p, v, pm, _ = nb.ic_plummer(n, 31)
+    m = pm[:, 3].copy()
+    s = nb.System(n, nb.INTEGRATOR_KDK64, EPS2, dt, 1.0)
+    s.set_state64(p, v, m)
+    s.step(steps)
+    ps, vs = s.get_state64()
+    s.close()
+    e = nb.Ensemble(n, 1, EPS2)
+    slot = e.add(p, v, m, dt, steps)
+    e.tick(steps + 1)
+    e.synchronize()
+    assert e.finished() == [slot]
+    pe, ve, _ = e.get_state(slot)
+    e.close()
+    # different kernel plans round differently; after 20 smooth steps the
+    # states agree to a few ulp-scale relative errors
+    assert np.abs(pe - ps).max() <= 1e-9 * np.abs(ps).max()
+    assert np.abs(ve - vs).max() <= 1e-8 * np.abs(vs).max()
+
+
+def test_admission_limits_and_reuse(cuda):
+    e = nb.Ensemble(5000, 3, EPS2)
+    p, v, m, _ = _ball(2000, 1)
+    a = e.add(p, v, m, 0.01, 2)
+    b = e.add(p, v, m, 0.01, 2)
+    assert a is not None and b is not None
+    assert e.add(p, v, m, 0.01, 2) is None  # bodies exhausted
+    q, w, mm, _ = _ball(500, 2)
+    c = e.add(q, w, mm, 0.01, 1)
+    assert c is not None
+    assert e.add(q, w, mm, 0.01, 1) is None  # slots exhausted
+    e.tick(3)
+    e.synchronize()
+    assert sorted(e.finished()) == sorted([a, b, c])
+    e.remove(a)
+    assert e.add(p, v, m, 0.01, 1) is not None  # space reused
+    assert e.active() == 3
+    e.close()
+
+
+def test_energy_conserved_in_ensemble(cuda):
+    n = 2048
+    p, v, pm, _ = nb.ic_plummer(n, 44)
+    m = pm[:, 3].copy()
+    e = nb.Ensemble(3 * n, 3, EPS2)
+    slot = e.add(p, v, m, 0.002, 200)
+    e.tick(201)
+    e.synchronize()
+    p1, v1, _ = e.get_state(slot)
+    e.close()
+
+    def energy(pos, vel):
+        pm4 = np.zeros((n, 4), np.float32)
+        pm4[:, :3] = pos
+        pm4[:, 3] = m
+        phi = O.ieee().potential_f64(pm4, float(np.float32(EPS2)))
+        return 0.5 * (m * (vel ** 2).sum(1)).sum() + 0.5 * (m * phi).sum()
+
+    e0, e1 = energy(p, v), energy(p1, v1)
+    assert abs(e1 - e0) / abs(e0) < 1e-4
