@@ -471,6 +471,7 @@ struct nbgb_ensemble {
     bool dirty = true;
     cudaGraphExec_t graph = nullptr;
     bool use_graph = true;
+    int stable_ticks = 0;  // ticks since the membership last changed
     int grid = 0;
     size_t bytes_total = 0;
     long long ticks = 0;
@@ -525,7 +526,11 @@ void fill_desc(nbgb_ensemble *e, int slot, Desc &d) {
 }
 
 // Rebuild descriptors, the j-stream slot map and the largest-first item list.
+// The pinned staging buffers are re-filled, so uploads (and ticks) still queued
+// from an earlier rebuild must have run first: synchronise the stream.
 int rebuild(nbgb_ensemble *e) {
+    if (cudaStreamSynchronize(e->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
     struct It {
         int4 v;
         double cost;
@@ -814,8 +819,11 @@ NBGB_API int nbgb_ensemble_tick(nbgb_ensemble *e, int nticks) {
             int rc = rebuild(e);
             if (rc != NBGB_OK)
                 return rc;
+            e->stable_ticks = 0;
         }
-        if (e->use_graph) {
+        // A graph pays off only when it is replayed: capture it once the
+        // membership has been unchanged for two ticks, launch eagerly before.
+        if (e->use_graph && e->stable_ticks >= 2) {
             if (!e->graph) {
                 cudaGraph_t g = nullptr;
                 if (cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal) !=
@@ -840,6 +848,7 @@ NBGB_API int nbgb_ensemble_tick(nbgb_ensemble *e, int nticks) {
             if (rc != NBGB_OK)
                 return rc;
         }
+        e->stable_ticks++;
         e->ticks++;
         // host bookkeeping of this tick
         for (auto &h : e->sys) {
