@@ -170,6 +170,22 @@ def cpu_rate(pm: np.ndarray, seconds: float):
     return rate, el, info
 
 
+def profiled_traffic(config_name: str, n: int, nsplit: int):
+    """DRAM bytes per force launch from the committed ncu summary, when it was
+    captured for this kernel configuration, N and j-split (else None)."""
+    path = os.path.join(ROOT, "profiles", "force_kernel_n1048576_dram.md")
+    if not os.path.exists(path):
+        return None
+    import re
+    for line in open(path):
+        m = re.match(r"traffic_bytes_per_launch:\s*(\d+)\s+config\s+(\S+)\s+n\s+(\d+)"
+                     r"\s+nsplit\s+(\d+)", line.strip())
+        if m and m.group(2) == config_name and int(m.group(3)) == n and \
+                int(m.group(4)) == nsplit:
+            return int(m.group(1))
+    return None
+
+
 def run_reference_arm(args, ws, rank):
     if rank != 0:
         return
@@ -275,6 +291,8 @@ def run_gb300(args, ws, rank, local):
     kernel_ms = float(np.mean(force_ms))
     achieved = FLOP * float(n) * float(n) / (kernel_ms * 1e-3)
     cfg, nsplit = sysm.plan()
+    cfg_name = nb.force_config_names()[cfg]
+    traffic = profiled_traffic(cfg_name, n, nsplit)
     sysm.close()
 
     # e2e: the drop-in entry point with host buffers
@@ -308,12 +326,15 @@ def run_gb300(args, ws, rank, local):
         "data": "synthetic (seeded Plummer sphere, G=M=a=1)",
         "config": {"workload": f"plain large system: N={n:,} Plummer, FP32 force, "
                                "FP64 KDK integrate, eps2=1e-4, dt=0.005",
-                   "n_bodies": n, "integrator": "kdk64", "force_config":
-                       nb.force_config_names()[cfg], "nsplit": nsplit,
+                   "n_bodies": n, "integrator": "kdk64", "force_config": cfg_name,
+                   "nsplit": nsplit,
                    "l2": "flushed between steps (256 MiB write outside the step events)",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fp32_peak / 1e12,
-                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
+                     "traffic_unit": "bytes per launch (ncu dram read+write, "
+                                     "profiles/force_kernel_n1048576_dram.md)",
+                     "algorithmic_bytes": 48 * n,  # read targets + sources, write forces
                      "peak_source": "measured on this GPU by nbgb_measure_peak "
                                     f"(FFMA {ffma / 1e12:.2f}, FFMA2 {ffma2 / 1e12:.2f} "
                                     "TFLOP/s; FMA = 2 FLOP)",

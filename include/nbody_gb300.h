@@ -185,8 +185,8 @@ NBGB_API nbgb_ensemble *nbgb_ensemble_create(size_t max_bodies, int max_systems,
 NBGB_API void nbgb_ensemble_destroy(nbgb_ensemble *ens);
 NBGB_API size_t nbgb_ensemble_device_bytes(nbgb_ensemble *ens);
 /* Plan for N in [2^bucket, 2^(bucket+1)): variant 0..3 = (targets per
-   thread, unroll) (1,8) (2,4) (1,4) (2,8); tile 16..1024 bodies (multiple of
-   16); j-split 1..4; variant -1 = the default rule. */
+   thread, unroll) (1,8) (2,4) (1,4) (2,8); tile a power of two in 16..1024
+   bodies; j-split 1..4; variant -1 = the default rule. */
 NBGB_API int nbgb_ensemble_set_bucket_plan(nbgb_ensemble *ens, int bucket, int variant, int jt,
                                            int nsplit);
 /* Admit a system (HOST double[n][3] x, v; float m[n]); NBGB_ERR_NO_MEMORY if

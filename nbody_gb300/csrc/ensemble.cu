@@ -139,27 +139,31 @@ __device__ bool process_item(const Params &P, const Desc &d, int ib, int r, unsi
         }
         const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(ring + (size_t)s * kMaxJT);
         f2 ax[K], ay[K], az[K];
-#pragma unroll
-        for (int k = 0; k < K; k++)
-            ax[k] = ay[k] = az[k] = zero2;
-#pragma unroll UNROLL
-        for (int q = 0; q < jt / 2; q++) {
-            const ulonglong2 a = tp[2 * q];
-            const ulonglong2 b = tp[2 * q + 1];
+        // fold into the compensated sum every 256 sources (or per tile)
+        const int fpairs = jt / 2 < 128 ? jt / 2 : 128;
+        for (int q0 = 0; q0 < jt / 2; q0 += fpairs) {
 #pragma unroll
             for (int k = 0; k < K; k++)
-                pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p, ax[k], ay[k],
-                               az[k]);
-        }
+                ax[k] = ay[k] = az[k] = zero2;
+#pragma unroll UNROLL
+            for (int q = q0; q < q0 + fpairs; q++) {
+                const ulonglong2 a = tp[2 * q];
+                const ulonglong2 b = tp[2 * q + 1];
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            float l, h;
-            f2_unpack(ax[k], l, h);
-            comp_add(hx[k], lx[k], l + h);
-            f2_unpack(ay[k], l, h);
-            comp_add(hy[k], ly[k], l + h);
-            f2_unpack(az[k], l, h);
-            comp_add(hz[k], lz[k], l + h);
+                for (int k = 0; k < K; k++)
+                    pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p, ax[k],
+                                   ay[k], az[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                float l, h;
+                f2_unpack(ax[k], l, h);
+                comp_add(hx[k], lx[k], l + h);
+                f2_unpack(ay[k], l, h);
+                comp_add(hy[k], ly[k], l + h);
+                f2_unpack(az[k], l, h);
+                comp_add(hz[k], lz[k], l + h);
+            }
         }
         __syncwarp();
         if (lane == 0) {
@@ -721,14 +725,15 @@ NBGB_API void nbgb_ensemble_destroy(nbgb_ensemble *e) {
 NBGB_API size_t nbgb_ensemble_device_bytes(nbgb_ensemble *e) { return e ? e->bytes_total : 0; }
 
 // Per-bucket plan (bucket b: N in [2^b, 2^(b+1))): variant 0..3 (targets per
-// thread and unroll: (1,8) (2,4) (1,4) (2,8)), tile 16..1024 bodies (multiple
-// of 16), j-split >= 1; variant -1 restores the default rule.  Applies to
-// systems admitted afterwards.
+// thread and unroll: (1,8) (2,4) (1,4) (2,8)), tile a power of two in
+// 16..1024 bodies, j-split 1..4; variant -1 restores the default rule.
+// Applies to systems admitted afterwards.
 NBGB_API int nbgb_ensemble_set_bucket_plan(nbgb_ensemble *e, int bucket, int variant, int jt,
                                            int nsplit) {
     if (!e || bucket < 0 || bucket >= 32 || variant < -1 || variant > 3)
         return NBGB_ERR_INVALID_ARGUMENT;
-    if (variant >= 0 && (jt < 16 || jt > nbgb::ens::kMaxJT || jt % 16 || nsplit < 1 || nsplit > 4))
+    if (variant >= 0 &&
+        (jt < 16 || jt > nbgb::ens::kMaxJT || (jt & (jt - 1)) || nsplit < 1 || nsplit > 4))
         return NBGB_ERR_INVALID_ARGUMENT;
     e->bucket[bucket].variant = variant;
     e->bucket[bucket].jt = jt;

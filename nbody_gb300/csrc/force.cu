@@ -19,8 +19,8 @@
 //                  ring completing on mbarriers, read back with broadcast
 //                  128-bit shared loads, and evaluated two interactions per
 //                  instruction with the f32x2 FP32 instructions (rsqrt on the
-//                  MUFU pipe).  Each tile's FP32 partial sum is folded into a
-//                  per-body compensated (TwoSum) running sum.
+//                  MUFU pipe).  Every 256 sources the FP32 partial sum is
+//                  folded into a per-body compensated (TwoSum) running sum.
 //                  With nsplit > 1 the j-range of an i-block is cut into
 //                  nsplit slices so that the number of units fills the GPU's
 //                  SMs evenly.  Each unit writes its (hi, lo) partials; the
@@ -111,6 +111,10 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     constexpr uint32_t TILE_BYTES = JT * 16u * VPB;
     static_assert(JT % 2 == 0, "tiles hold whole pairs");
     static_assert(MODE != 4 || K % 2 == 0, "targets are paired");
+    // Sources summed in plain FP32 before each fold into the compensated
+    // (TwoSum) sum: at most 256 (128 per f32x2 half), whatever the tile size.
+    constexpr int FLUSH = JT < 256 ? JT : 256;
+    static_assert(JT % FLUSH == 0, "tiles hold whole flush chunks");
 
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *ring = reinterpret_cast<float4 *>(smem_raw);
@@ -207,10 +211,12 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                 constexpr int KP = K / 2 > 0 ? K / 2 : 1;
                 f2 ax[KP], ay[KP], az[KP];
 #pragma unroll
+                for (int j0 = 0; j0 < JT; j0 += FLUSH) {
+#pragma unroll
                 for (int c = 0; c < K / 2; c++)
                     ax[c] = ay[c] = az[c] = zero2;
 #pragma unroll UNROLL
-                for (int j = 0; j < JT; j++) {
+                for (int j = j0; j < j0 + FLUSH; j++) {
                     const ulonglong2 a = tp[2 * j];      // (x,x) (y,y)
                     const ulonglong2 b = tp[2 * j + 1];  // (z,z) (m,m)
 #pragma unroll
@@ -231,13 +237,15 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                     comp_add(hz[2 * c], lz[2 * c], l);
                     comp_add(hz[2 * c + 1], lz[2 * c + 1], h);
                 }
+                }
             } else if constexpr (POT) {  // packed f32x2 with the potential
                 f2 ax[K], ay[K], az[K], ap[K];
+                for (int q0 = 0; q0 < JT / 2; q0 += FLUSH / 2) {
 #pragma unroll
                 for (int k = 0; k < K; k++)
                     ax[k] = ay[k] = az[k] = ap[k] = zero2;
 #pragma unroll UNROLL
-                for (int q = 0; q < JT / 2; q++) {
+                for (int q = q0; q < q0 + FLUSH / 2; q++) {
                     const ulonglong2 a = tp[2 * q];
                     const ulonglong2 b = tp[2 * q + 1];
 #pragma unroll
@@ -257,13 +265,15 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                     f2_unpack(ap[k], l, h);
                     comp_add(hp[k], lp[k], l + h);
                 }
+                }
             } else if constexpr (MODE != 0) {  // packed f32x2 (MODE 2: all ops as FMAs)
                 f2 ax[K], ay[K], az[K];
+                for (int q0 = 0; q0 < JT / 2; q0 += FLUSH / 2) {
 #pragma unroll
                 for (int k = 0; k < K; k++)
                     ax[k] = ay[k] = az[k] = zero2;
 #pragma unroll UNROLL
-                for (int q = 0; q < JT / 2; q++) {
+                for (int q = q0; q < q0 + FLUSH / 2; q++) {
                     const ulonglong2 a = tp[2 * q];
                     const ulonglong2 b = tp[2 * q + 1];
 #pragma unroll
@@ -286,14 +296,16 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                     f2_unpack(az[k], l, h);
                     comp_add(hz[k], lz[k], l + h);
                 }
+                }
             } else {
                 float ax[K], ay[K], az[K];
+                const float4 *tf = reinterpret_cast<const float4 *>(tp);
+                for (int q0 = 0; q0 < JT / 2; q0 += FLUSH / 2) {
 #pragma unroll
                 for (int k = 0; k < K; k++)
                     ax[k] = ay[k] = az[k] = 0.f;
-                const float4 *tf = reinterpret_cast<const float4 *>(tp);
 #pragma unroll UNROLL
-                for (int q = 0; q < JT / 2; q++) {
+                for (int q = q0; q < q0 + FLUSH / 2; q++) {
                     const float4 a = tf[2 * q];      // x0 x1 y0 y1
                     const float4 b = tf[2 * q + 1];  // z0 z1 m0 m1
 #pragma unroll
@@ -309,6 +321,7 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                     comp_add(hx[k], lx[k], ax[k]);
                     comp_add(hy[k], ly[k], ay[k]);
                     comp_add(hz[k], lz[k], az[k]);
+                }
                 }
             }
         }
