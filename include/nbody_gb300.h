@@ -264,6 +264,10 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
    NBGB_STATUS_*).  Returns the bits, or a negative NBGB_ERR_* code. */
 NBGB_API int nbgb_last_status(void);
 NBGB_API const char *nbgb_status_string(int code);
+/* Self-test of the bounded waits: a kernel waits on an mbarrier that nothing
+   completes, gives up after limit_ms (0 < limit_ms <= 1000) and returns;
+   returns the status bits it left (NBGB_STATUS_WAIT_TIMEOUT expected). */
+NBGB_API int nbgb_selftest_bounded_wait(double limit_ms);
 /* Library / build identification. */
 NBGB_API const char *nbgb_version(void);
 

@@ -87,6 +87,7 @@ SIGNATURES = {
     "nbgb_last_status": (ctypes.c_int, []),
     "nbgb_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "nbgb_version": (ctypes.c_char_p, []),
+    "nbgb_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_double]),
 }
 
 _lib = None

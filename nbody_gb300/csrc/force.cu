@@ -694,6 +694,21 @@ int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cud
 const char *config_name(int c) { return (c >= 0 && c < kNumConfigs) ? kConfigs[c].name : "?"; }
 int num_configs() { return kNumConfigs; }
 
+// Self-test of the bounded-wait path: one CTA waits on an mbarrier that
+// nothing ever completes, with a limit of limit_ns; the wait gives up, sets
+// NBGB_STATUS_WAIT_TIMEOUT and the kernel returns normally.
+__global__ void selftest_wait_kernel(unsigned long long limit_ns, int *out) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&bar, 0u, limit_ns);
+    if (threadIdx.x == 0)
+        *out = ok ? 1 : 0;
+}
+
 static NBGB_STATUS_READER(read_status_force)
 
 int read_and_clear_status(unsigned *bits) {
@@ -886,5 +901,30 @@ NBGB_API const char *nbgb_status_string(int code) {
 }
 
 NBGB_API const char *nbgb_version(void) { return "nbody_gb300 0.1 (sm_103a)"; }
+
+// Runs the bounded-wait self-test (limit in milliseconds, 0 < limit <= 1000)
+// and returns the device status bits it left (NBGB_STATUS_WAIT_TIMEOUT
+// expected), or a negative NBGB_ERR_* code.  Synchronous.
+NBGB_API int nbgb_selftest_bounded_wait(double limit_ms) {
+    if (!(limit_ms > 0.0) || limit_ms > 1000.0)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    int *out = nullptr, h = -1;
+    unsigned bits = 0;
+    if (read_and_clear_status(&bits) != NBGB_OK)  // start from a clean word
+        return NBGB_ERR_CUDA;
+    if (cudaMalloc(&out, sizeof(int)) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    selftest_wait_kernel<<<1, 32>>>((unsigned long long)(limit_ms * 1e6), out);
+    int rc = NBGB_OK;
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(&h, out, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = NBGB_ERR_CUDA;
+    cudaFree(out);
+    if (rc != NBGB_OK)
+        return rc;
+    if (read_and_clear_status(&bits) != NBGB_OK)
+        return NBGB_ERR_CUDA;
+    return h == 0 ? (int)bits : NBGB_ERR_DEVICE;
+}
 
 }  // extern "C"
