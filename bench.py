@@ -88,6 +88,14 @@ def _allsum(ws, x: float) -> float:
     return float(t.item())
 
 
+def aggregate(ws: int, seconds: float, interactions: float):
+    """Whole-job rate of independent replicas: every rank's interactions
+    over the slowest rank's time (1e9 interactions/s), and that time."""
+    t_max = _allmax(ws, seconds)
+    total = _allsum(ws, interactions)
+    return total / t_max / 1e9, t_max, total
+
+
 # ---------------------------------------------------------------------------
 # nvidia-smi clock sampling during the timed region
 # ---------------------------------------------------------------------------
@@ -253,6 +261,8 @@ def run_gb300(args, ws, rank, local):
     p3, v3, pm_np, _ = nb.ic_plummer(n, SEED + rank)
     sysm = nb.System(n, nb.INTEGRATOR_KDK64, EPS2, DT, 1.0)
     sysm.set_state64(p3, v3, pm_np[:, 3].copy())
+    if args.force == "newton3":
+        sysm.set_force_algorithm("newton3")
     sysm.set_timing(True)
     stream = torch.cuda.ExternalStream(sysm.stream, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -284,14 +294,12 @@ def run_gb300(args, ws, rank, local):
     sysm.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_dev = sum(step_ms) / 1e3
-    t_max = _allmax(ws, t_dev)
     inter = float(n) * float(n) * args.steps
-    total_inter = _allsum(ws, inter)
-    value = total_inter / t_max / 1e9
+    value, t_max, total_inter = aggregate(ws, t_dev, inter)
     kernel_ms = float(np.mean(force_ms))
     achieved = FLOP * float(n) * float(n) / (kernel_ms * 1e-3)
     cfg, nsplit = sysm.plan()
-    cfg_name = nb.force_config_names()[cfg]
+    cfg_name = nb.force_config_names()[cfg] if args.force == 'onesided' else 'newton3'
     traffic = profiled_traffic(cfg_name, n, nsplit)
     sysm.close()
 
@@ -316,8 +324,7 @@ def run_gb300(args, ws, rank, local):
         torch.cuda.synchronize()
     e2e_t = time.perf_counter() - t0
     assert min(ms_calls) > 0.0, "drop-in entry point reported failure"
-    e2e_t = _allmax(ws, e2e_t)
-    e2e_value = total_inter / e2e_t / 1e9
+    e2e_value, e2e_t, _ = aggregate(ws, e2e_t, inter)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -362,6 +369,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--force", choices=["onesided", "newton3"], default="onesided",
+                    help="force algorithm of the timed steps")
     ap.add_argument("--n", type=int, default=N_BODIES,
                     help="bodies (default 1,048,576; smaller only for profiling captures)")
     args = ap.parse_args()

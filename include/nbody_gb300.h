@@ -77,6 +77,17 @@ NBGB_API int nbgb_force_ex(float *force, const float *posMass, float softeningSq
                            void *workspace, size_t workspace_bytes, int config, int nsplit,
                            void *stream);
 
+/*
+ * Newton's-third-law variant (the reference's unregistered tiled kernels,
+ * src/nbody_GPU_AOS_tiled.cu:93-179, compute each pair once too): each pair
+ * is evaluated once and applied to both bodies; per-block-pair sums are
+ * accumulated in FP64 and rounded to FP32 at the end.  Same arguments and
+ * conventions as nbgb_force; workspace >= nbgb_force_newton3_workspace_bytes.
+ */
+NBGB_API size_t nbgb_force_newton3_workspace_bytes(size_t N);
+NBGB_API int nbgb_force_newton3(float *force, const float *posMass, float softeningSquared,
+                                size_t N, void *workspace, size_t workspace_bytes, void *stream);
+
 /* The planner's decision for N (config / nsplit forced when >= 0). */
 NBGB_API int nbgb_force_plan(size_t N, int config, int nsplit, int *out_config, int *out_nsplit,
                              size_t *out_workspace_bytes);
@@ -145,6 +156,8 @@ NBGB_API int nbgb_system_set_state64(nbgb_system *sys, const double *pos3, const
 /* Advance nsteps (asynchronous; reference steps replay one CUDA graph). */
 NBGB_API int nbgb_system_step(nbgb_system *sys, int nsteps);
 NBGB_API int nbgb_system_set_graph(nbgb_system *sys, int enable);
+/* 0: one-sided force kernel (default); 1: Newton's-third-law variant. */
+NBGB_API int nbgb_system_set_force_algorithm(nbgb_system *sys, int algorithm);
 /* Bracket every force launch with CUDA events on the system's stream (steps
    then run eagerly); nbgb_system_last_force_ms reads the latest one. */
 NBGB_API int nbgb_system_set_timing(nbgb_system *sys, int enable);

@@ -134,6 +134,23 @@ def force(posMass, softeningSquared: float, out=None, stream=None, workspace: Wo
     return out
 
 
+def force_newton3(posMass, softeningSquared: float, out=None, stream=None,
+                  workspace: Workspace = None):
+    """Same sum as force(), each pair evaluated once (Newton's third law)."""
+    torch = _torch()
+    n = posMass.shape[0]
+    if out is None:
+        out = torch.empty((n, 4), dtype=torch.float32, device=posMass.device)
+    if n == 0:
+        return out
+    lib = load()
+    wsb = lib.nbgb_force_newton3_workspace_bytes(n)
+    ws = (workspace or _default_ws).get(wsb)
+    check(lib.nbgb_force_newton3(_dev(out), _dev(posMass), softeningSquared, n, ws.data_ptr(),
+                                 ws.numel(), _stream(stream)), "nbgb_force_newton3")
+    return out
+
+
 def integrate_reference(posMass, velInvMass, force_, dt: float, damping: float, stream=None):
     """In place on (N,4) float32 CUDA tensors (src/nbody.cu:158-182)."""
     n = posMass.shape[0]
@@ -202,6 +219,11 @@ class System:
 
     def use_graph(self, enable: bool):
         check(self.lib.nbgb_system_set_graph(self.h, int(enable)), "set_graph")
+
+    def set_force_algorithm(self, name: str):
+        """'onesided' (default) or 'newton3'."""
+        code = {"onesided": 0, "newton3": 1}[name]
+        check(self.lib.nbgb_system_set_force_algorithm(self.h, code), "set_force_algorithm")
 
     def synchronize(self):
         check(self.lib.nbgb_system_synchronize(self.h), "synchronize")

@@ -27,6 +27,9 @@ SIGNATURES = {
     "nbgb_force": (ctypes.c_int, [c_vp, c_vp, ctypes.c_float, c_size, c_vp, c_size, c_vp]),
     "nbgb_force_ex": (ctypes.c_int, [c_vp, c_vp, ctypes.c_float, c_size, c_vp, c_size,
                                      ctypes.c_int, ctypes.c_int, c_vp]),
+    "nbgb_force_newton3_workspace_bytes": (c_size, [c_size]),
+    "nbgb_force_newton3": (ctypes.c_int, [c_vp, c_vp, ctypes.c_float, c_size, c_vp, c_size,
+                                          c_vp]),
     "nbgb_force_plan": (ctypes.c_int, [c_size, ctypes.c_int, ctypes.c_int, c_intp, c_intp,
                                        c_sizep]),
     "nbgb_force_num_configs": (ctypes.c_int, []),
@@ -44,6 +47,7 @@ SIGNATURES = {
     "nbgb_system_set_state64": (ctypes.c_int, [c_vp, c_f64p, c_f64p, c_f32p]),
     "nbgb_system_step": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "nbgb_system_set_graph": (ctypes.c_int, [c_vp, ctypes.c_int]),
+    "nbgb_system_set_force_algorithm": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "nbgb_system_synchronize": (ctypes.c_int, [c_vp]),
     "nbgb_system_set_timing": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "nbgb_system_last_force_ms": (ctypes.c_int, [c_vp, c_f32p]),

@@ -1,0 +1,314 @@
+// force_sym.cu -- the all-pairs force with Newton's third law: every pair of
+// bodies is evaluated once and applied to both (the idea of the reference's
+// unregistered tiled kernels, src/nbody_GPU_AOS_tiled.cu:93-179, which add
+// every pair's contribution with per-pair warp reductions and float atomics).
+//
+// Here the unit of work is a block pair (bi, bj), bi <= bj, of 1024-body
+// blocks, one CTA of 8 warps each:
+//   * warp w holds 128 targets of block bi in registers (4 per lane, negated
+//     and duplicated into f32x2 pairs, with their masses);
+//   * block bj is visited as 8 source sets of 128 bodies; every lane loads 4
+//     sources (2 f32x2 pairs of the j-stream) plus zeroed accumulators, and
+//     for 32 steps evaluates its 4 targets against the 4 sources it holds,
+//     then passes sources and their accumulators to the next lane
+//     (__shfl_sync rotation).  After 32 steps each source has met every
+//     target of the warp and is back in its lane with its accumulated
+//     reaction;
+//   * per pair and target: d = p_j - p_i, s = (|d|^2 + eps2)^-3/2 (MUFU
+//     rsqrt), a_i += m_j s d, a_j -= m_i s d: 16 f32x2 operations per 4
+//     interactions instead of 24 for the one-sided kernel;
+//   * the 8 warps' reactions on a source set are added in shared memory in
+//     warp order (deterministic), then one FP64 atomic add per body and
+//     component moves them to the global FP64 accumulator; the targets'
+//     sums (compensated, FP32 TwoSum every 256 sources) are added the same
+//     way at the end of the block pair;
+//   * diagonal block pairs (bi == bj): warp w skips source sets s < w and
+//     evaluates s == w one-sided (every ordered pair of the set once, the
+//     self pair contributing 0).
+// A final kernel rounds the FP64 accumulators to FP32 forces.  The FP64 sums
+// receive ~2 N / 1024 contributions per body in an order set by scheduling;
+// FP64 keeps the result order-independent to well below FP32 resolution.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "nbgb_device.cuh"
+#include "nbgb_internal.h"
+#include "nbody_gb300.h"
+
+namespace nbgb {
+namespace sym {
+
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+constexpr int KI = 4;                        // targets per lane
+constexpr int KJ = 4;                        // sources per lane (2 f32x2 pairs)
+constexpr int kSet = 32 * KJ;                // sources per set
+constexpr int kBlock = kWarps * 32 * KI;     // bodies per block (1024)
+static_assert(kBlock == kWarps * kSet, "a block is 8 source sets");
+
+struct Params {
+    const float4 *__restrict__ pm;  // AOS posMass (targets), n bodies
+    const float4 *__restrict__ js;  // paired j-stream, npad bodies
+    double *__restrict__ acc;       // [3][npad] FP64 accumulators
+    int n, npad, nblocks;
+    float eps2;
+};
+
+// pair index p -> (bi, bj) with bi <= bj over an nb x nb upper triangle,
+// rows of decreasing length.
+__device__ __forceinline__ void pair_of(long long p, int nb, int &bi, int &bj) {
+    // row r holds nb - r pairs; rows before r hold r*nb - r(r-1)/2
+    double b = 2.0 * nb + 1.0;
+    int r = (int)((b - sqrt(b * b - 8.0 * (double)p)) * 0.5);
+    if (r < 0)
+        r = 0;
+    if (r >= nb)
+        r = nb - 1;
+    auto start = [&](int rr) { return (long long)rr * nb - (long long)rr * (rr - 1) / 2; };
+    while (r > 0 && start(r) > p)
+        r--;
+    while (r + 1 < nb && start(r + 1) <= p)
+        r++;
+    bi = r;
+    bj = r + (int)(p - start(r));
+}
+
+// 32 rotation steps over one source set.  REACT: also accumulate the
+// sources' reactions (both sides); otherwise only the targets' sums.  The
+// branch on REACT is resolved at compile time, outside the step loop.
+template <bool REACT>
+__device__ __forceinline__ void rotate_set(f2 (&sx)[2], f2 (&sy)[2], f2 (&sz)[2], f2 (&sm)[2],
+                                           f2 (&rx)[2], f2 (&ry)[2], f2 (&rz)[2],
+                                           const f2 (&nx)[KI], const f2 (&ny)[KI],
+                                           const f2 (&nz)[KI], const f2 (&nm)[KI], f2 (&ax)[KI],
+                                           f2 (&ay)[KI], f2 (&az)[KI], f2 eps2p, int lane) {
+    const int from = (lane + 1) & 31;
+#pragma unroll 2
+    for (int step = 0; step < 32; step++) {
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+#pragma unroll
+            for (int k = 0; k < KI; k++) {
+                f2 dx = f2_add(sx[c], nx[k]);
+                f2 dy = f2_add(sy[c], ny[k]);
+                f2 dz = f2_add(sz[c], nz[k]);
+                f2 d2 = f2_fma(dx, dx, eps2p);
+                d2 = f2_fma(dy, dy, d2);
+                d2 = f2_fma(dz, dz, d2);
+                float d2l, d2h;
+                f2_unpack(d2, d2l, d2h);
+                const f2 inv = f2_pack(rsqrt_mufu(d2l), rsqrt_mufu(d2h));
+                const f2 inv2 = f2_mul(inv, inv);
+                const f2 sc = f2_mul(inv, inv2);  // (|d|^2+eps2)^-3/2
+                const f2 wi = f2_mul(sm[c], sc);  // m_j s
+                ax[k] = f2_fma(dx, wi, ax[k]);
+                ay[k] = f2_fma(dy, wi, ay[k]);
+                az[k] = f2_fma(dz, wi, az[k]);
+                if (REACT) {
+                    const f2 wj = f2_mul(nm[k], sc);  // -m_i s
+                    rx[c] = f2_fma(dx, wj, rx[c]);
+                    ry[c] = f2_fma(dy, wj, ry[c]);
+                    rz[c] = f2_fma(dz, wj, rz[c]);
+                }
+            }
+        }
+        // pass sources (and their reactions) to the next lane
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            sx[c] = __shfl_sync(0xffffffffu, sx[c], from);
+            sy[c] = __shfl_sync(0xffffffffu, sy[c], from);
+            sz[c] = __shfl_sync(0xffffffffu, sz[c], from);
+            sm[c] = __shfl_sync(0xffffffffu, sm[c], from);
+            if (REACT) {
+                rx[c] = __shfl_sync(0xffffffffu, rx[c], from);
+                ry[c] = __shfl_sync(0xffffffffu, ry[c], from);
+                rz[c] = __shfl_sync(0xffffffffu, rz[c], from);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 2) sym_kernel(Params P) {
+    __shared__ float red[kWarps][3][kSet];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    int bi, bj;
+    pair_of(blockIdx.x, P.nblocks, bi, bj);
+    const bool diag = (bi == bj);
+
+    // targets: lane owns bodies bi*1024 + warp*128 + lane + 32*k
+    f2 nx[KI], ny[KI], nz[KI], nm[KI];
+    f2 ax[KI], ay[KI], az[KI];
+    float hx[KI], hy[KI], hz[KI], lx[KI], ly[KI], lz[KI];
+#pragma unroll
+    for (int k = 0; k < KI; k++) {
+        const int i = bi * kBlock + warp * 32 * KI + lane + 32 * k;
+        const float4 b = (i < P.n) ? P.pm[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        nx[k] = f2_pack(-b.x, -b.x);
+        ny[k] = f2_pack(-b.y, -b.y);
+        nz[k] = f2_pack(-b.z, -b.z);
+        nm[k] = f2_pack(-b.w, -b.w);
+        hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
+    }
+    const f2 eps2p = f2_pack(P.eps2, P.eps2);
+    const f2 zero2 = f2_pack(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < KI; k++)
+        ax[k] = ay[k] = az[k] = zero2;
+
+    for (int s = 0; s < kWarps; s++) {
+        // mode: 2 both sides, 1 targets only (the warp's own set), 0 skip
+        const int mode = !diag ? 2 : (s > warp ? 2 : (s == warp ? 1 : 0));
+        // sources of set s: lane holds bodies base + lane*4 .. +3 (2 pairs)
+        const int base = bj * kBlock + s * kSet + lane * KJ;
+        f2 sx[2], sy[2], sz[2], sm[2], rx[2], ry[2], rz[2];
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            const ulonglong2 a = reinterpret_cast<const ulonglong2 *>(P.js)[base + 2 * c];
+            const ulonglong2 b = reinterpret_cast<const ulonglong2 *>(P.js)[base + 2 * c + 1];
+            sx[c] = a.x;
+            sy[c] = a.y;
+            sz[c] = b.x;
+            sm[c] = b.y;
+            rx[c] = ry[c] = rz[c] = zero2;
+        }
+        if (mode == 2)
+            rotate_set<true>(sx, sy, sz, sm, rx, ry, rz, nx, ny, nz, nm, ax, ay, az, eps2p, lane);
+        else if (mode == 1)
+            rotate_set<false>(sx, sy, sz, sm, rx, ry, rz, nx, ny, nz, nm, ax, ay, az, eps2p, lane);
+        // fold target sums into the compensated sums every 2 sets (256 sources)
+        if (s & 1) {
+#pragma unroll
+            for (int k = 0; k < KI; k++) {
+                float l, h;
+                f2_unpack(ax[k], l, h);
+                comp_add(hx[k], lx[k], l + h);
+                f2_unpack(ay[k], l, h);
+                comp_add(hy[k], ly[k], l + h);
+                f2_unpack(az[k], l, h);
+                comp_add(hz[k], lz[k], l + h);
+                ax[k] = ay[k] = az[k] = zero2;
+            }
+        }
+        // reactions on set s: stage per warp, add in warp order, FP64 atomics
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            float l, h;
+            f2_unpack(rx[c], l, h);
+            red[warp][0][lane * KJ + 2 * c] = l;
+            red[warp][0][lane * KJ + 2 * c + 1] = h;
+            f2_unpack(ry[c], l, h);
+            red[warp][1][lane * KJ + 2 * c] = l;
+            red[warp][1][lane * KJ + 2 * c + 1] = h;
+            f2_unpack(rz[c], l, h);
+            red[warp][2][lane * KJ + 2 * c] = l;
+            red[warp][2][lane * KJ + 2 * c + 1] = h;
+        }
+        __syncthreads();
+        for (int q = tid; q < 3 * kSet; q += kThreads) {
+            const int comp = q / kSet, jj = q - comp * kSet;
+            float t = 0.f;
+#pragma unroll
+            for (int w = 0; w < kWarps; w++)
+                t += red[w][comp][jj];
+            const int j = bj * kBlock + s * kSet + jj;
+            if (t != 0.f && j < P.n)
+                atomicAdd(&P.acc[(size_t)comp * P.npad + j], (double)t);
+        }
+        __syncthreads();
+    }
+    // targets' sums -> FP64 accumulators
+#pragma unroll
+    for (int k = 0; k < KI; k++) {
+        const int i = bi * kBlock + warp * 32 * KI + lane + 32 * k;
+        if (i < P.n) {
+            atomicAdd(&P.acc[i], (double)hx[k] + (double)lx[k]);
+            atomicAdd(&P.acc[(size_t)P.npad + i], (double)hy[k] + (double)ly[k]);
+            atomicAdd(&P.acc[2 * (size_t)P.npad + i], (double)hz[k] + (double)lz[k]);
+        }
+    }
+}
+
+__global__ void sym_finish_kernel(const double *__restrict__ acc, int n, int npad,
+                                  float4 *__restrict__ force) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        force[i] = make_float4((float)acc[i], (float)acc[(size_t)npad + i],
+                               (float)acc[2 * (size_t)npad + i], 0.f);
+}
+
+}  // namespace sym
+}  // namespace nbgb
+
+namespace {
+
+struct SymLayout {
+    int nblocks, npad;
+    size_t off_js, off_acc, bytes;
+};
+
+SymLayout sym_layout(size_t n) {
+    SymLayout L;
+    L.nblocks = (int)((n + nbgb::sym::kBlock - 1) / nbgb::sym::kBlock);
+    L.npad = L.nblocks * nbgb::sym::kBlock;
+    L.off_js = 0;
+    L.off_acc = ((size_t)L.npad * 16 + 255) / 256 * 256;
+    L.bytes = L.off_acc + (size_t)3 * L.npad * sizeof(double);
+    return L;
+}
+
+}  // namespace
+
+extern "C" {
+
+NBGB_API size_t nbgb_force_newton3_workspace_bytes(size_t N) {
+    if (N == 0 || N > nbgb::kMaxBodies)
+        return 0;
+    return sym_layout(N).bytes;
+}
+
+NBGB_API int nbgb_force_newton3(float *force, const float *posMass, float softeningSquared,
+                                size_t N, void *workspace, size_t workspace_bytes, void *stream) {
+    if (N == 0)
+        return NBGB_OK;
+    if (!force || !posMass || N > nbgb::kMaxBodies)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (((uintptr_t)force | (uintptr_t)posMass) & 15u)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const SymLayout L = sym_layout(N);
+    if (!workspace || workspace_bytes < L.bytes || ((uintptr_t)workspace & 255u))
+        return NBGB_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    // the j-stream (paired layout, zero-mass padding to whole blocks)
+    nbgb::ForcePlan pl;
+    pl.n = N;
+    pl.ntiles = L.nblocks;
+    pl.tile_bodies = nbgb::sym::kBlock;
+    pl.js_vpb = 1;
+    pl.nsplit = 1;
+    pl.off_js = L.off_js;
+    int rc = nbgb::launch_pack(pl, (const float4 *)posMass, ws, st);
+    if (rc != NBGB_OK)
+        return rc;
+    double *acc = (double *)(ws + L.off_acc);
+    if (cudaMemsetAsync(acc, 0, (size_t)3 * L.npad * sizeof(double), st) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    nbgb::sym::Params P;
+    P.pm = (const float4 *)posMass;
+    P.js = (const float4 *)(ws + L.off_js);
+    P.acc = acc;
+    P.n = (int)N;
+    P.npad = L.npad;
+    P.nblocks = L.nblocks;
+    P.eps2 = softeningSquared;
+    const long long pairs = (long long)L.nblocks * (L.nblocks + 1) / 2;
+    if (pairs > (1ll << 31) - 1)
+        return NBGB_ERR_TOO_LARGE;
+    nbgb::sym::sym_kernel<<<(unsigned)pairs, nbgb::sym::kThreads, 0, st>>>(P);
+    nbgb::sym::sym_finish_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(
+        acc, (int)N, L.npad, (float4 *)force);
+    return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
+}
+
+}  // extern "C"

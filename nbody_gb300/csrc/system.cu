@@ -47,6 +47,10 @@ struct nbgb_system {
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed_once = false;
+    // force algorithm: 0 one-sided (planned kernel), 1 Newton's third law
+    int algorithm = 0;
+    void *ws_n3 = nullptr;
+    size_t ws_n3_bytes = 0;
     // diagnostics (allocated on first use)
     ForcePlan diag_plan;
     void *diag_ws = nullptr;
@@ -77,6 +81,9 @@ int ensure_jstream(nbgb_system *s) {
 }
 
 int force_pass(nbgb_system *s) {
+    if (s->algorithm == 1)
+        return nbgb_force_newton3((float *)s->force, (const float *)s->pm, s->eps2, s->n,
+                                  s->ws_n3, s->ws_n3_bytes, s->stream);
     int rc = ensure_jstream(s);
     if (rc != NBGB_OK)
         return rc;
@@ -87,7 +94,11 @@ int force_pass(nbgb_system *s) {
 int timed_force(nbgb_system *s) {
     if (s->timing && cudaEventRecord(s->ev0, s->stream) != cudaSuccess)
         return NBGB_ERR_CUDA;
-    int rc = nbgb::launch_force(s->plan, s->force, s->pm, js_of(s), s->eps2, s->ws, s->stream);
+    int rc = s->algorithm == 1
+                 ? nbgb_force_newton3((float *)s->force, (const float *)s->pm, s->eps2, s->n,
+                                      s->ws_n3, s->ws_n3_bytes, s->stream)
+                 : nbgb::launch_force(s->plan, s->force, s->pm, js_of(s), s->eps2, s->ws,
+                                      s->stream);
     if (rc == NBGB_OK && s->timing) {
         if (cudaEventRecord(s->ev1, s->stream) != cudaSuccess)
             return NBGB_ERR_CUDA;
@@ -144,6 +155,7 @@ void free_all(nbgb_system *s) {
     cudaFree(s->mass);
     cudaFree(s->ws);
     cudaFree(s->diag_ws);
+    cudaFree(s->ws_n3);
     cudaFree(s->phi);
     cudaFree(s->diag_scratch);
     cudaFree(s->diag_out);
@@ -334,6 +346,27 @@ NBGB_API int nbgb_system_step(nbgb_system *s, int nsteps) {
         }
     }
     return half_kick(s);
+}
+
+// Force algorithm of the step loop: 0 the one-sided kernel (default), 1 the
+// Newton's-third-law variant (allocates its workspace on first selection).
+NBGB_API int nbgb_system_set_force_algorithm(nbgb_system *s, int algorithm) {
+    if (!s || algorithm < 0 || algorithm > 1)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (algorithm == 1 && !s->ws_n3) {
+        s->ws_n3_bytes = nbgb_force_newton3_workspace_bytes(s->n);
+        if (!s->ws_n3_bytes || cudaMalloc(&s->ws_n3, s->ws_n3_bytes) != cudaSuccess) {
+            s->ws_n3 = nullptr;
+            return NBGB_ERR_NO_MEMORY;
+        }
+    }
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    s->algorithm = algorithm;
+    s->accel_valid = false;
+    return NBGB_OK;
 }
 
 // Timing mode: every force launch is bracketed by CUDA events on the
