@@ -354,11 +354,53 @@ def run_gb300(args, ws, rank, local):
         "clocks": clk,
         "wall_s": wall,
     }
+    if args.force == "onesided" and not args.no_newton3:
+        line["newton3"] = measure_newton3(args, n, p3, v3, pm_np, dev, ffma, ffma2, fp32_peak,
+                                          flush)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         rate, el, info = cpu_rate(pm_np, args.cpu_seconds)
         line["cpu_baseline"] = dict(value=rate, unit=UNIT, **info)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def measure_newton3(args, n, p3, v3, pm_np, dev, ffma, ffma2, fp32_peak, flush):
+    """The same timed steps with the Newton's-third-law force variant (each
+    pair evaluated once), reported beside the headline kernel."""
+    import torch
+
+    import nbody_gb300 as nb
+    s = nb.System(n, nb.INTEGRATOR_KDK64, EPS2, DT, 1.0)
+    s.set_state64(p3, v3, pm_np[:, 3].copy())
+    s.set_force_algorithm("newton3")
+    s.set_timing(True)
+    stream = torch.cuda.ExternalStream(s.stream, device=dev)
+    for _ in range(args.warmup):
+        s.step(1)
+    s.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    fms = []
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev[k][0].record(stream)
+        s.step(1)
+        ev[k][1].record(stream)
+        fms.append(s.last_force_ms())
+    torch.cuda.synchronize()
+    s.synchronize()
+    s.close()
+    t = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    kms = float(np.mean(fms))
+    return {"value": float(n) * n * args.steps / t / 1e9, "unit": UNIT,
+            "ms_per_step": t * 1e3 / args.steps, "force_ms": kms,
+            "roofline_20flop_frac": FLOP * float(n) * n / (kms * 1e-3) / fp32_peak,
+            "executed_fp32_frac": 25 * (float(n) * n / 2) / (kms * 1e-3) / fp32_peak,
+            "note": "each pair evaluated once and applied to both bodies (16 FP32 "
+                    "operations = 25 FLOP per pair, FMA = 2, plus one rsqrt); the first "
+                    "fraction uses the reference's 20 FLOP per interaction, the second the "
+                    "FP32 work actually executed"}
 
 
 def main():
@@ -369,6 +411,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-newton3", action="store_true",
+                    help="skip the extra Newton's-third-law measurement")
     ap.add_argument("--force", choices=["onesided", "newton3"], default="onesided",
                     help="force algorithm of the timed steps")
     ap.add_argument("--n", type=int, default=N_BODIES,

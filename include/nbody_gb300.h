@@ -48,6 +48,13 @@ extern "C" {
 NBGB_API float ComputeGravitation_GPU_GB300(float *force, float *posMass, float softeningSquared,
                                             size_t N);
 
+/* A second row for the table, same signature and conventions: the
+   Newton's-third-law variant (nbgb_force_newton3), each pair evaluated once;
+   like the reference's unregistered tiled kernels
+   (src/nbody_GPU_AOS_tiled.cu:181-218). */
+NBGB_API float ComputeGravitation_GPU_GB300_Newton3(float *force, float *posMass,
+                                                    float softeningSquared, size_t N);
+
 /* Frees the drop-in entry point's cached scratch space on every device. */
 NBGB_API void nbgb_release_workspace(void);
 

@@ -82,6 +82,12 @@ def ComputeGravitation_GPU_GB300(force, posMass, softeningSquared: float, N: int
                                                      softeningSquared, N))
 
 
+def ComputeGravitation_GPU_GB300_Newton3(force, posMass, softeningSquared: float, N: int) -> float:
+    """The Newton's-third-law variant as a table row (same conventions)."""
+    return float(load().ComputeGravitation_GPU_GB300_Newton3(_dev(force), _dev(posMass),
+                                                            softeningSquared, N))
+
+
 def release_workspace() -> None:
     load().nbgb_release_workspace()
 

@@ -22,6 +22,8 @@ c_size = ctypes.c_size_t
 # name: (restype, argtypes)
 SIGNATURES = {
     "ComputeGravitation_GPU_GB300": (ctypes.c_float, [c_vp, c_vp, ctypes.c_float, c_size]),
+    "ComputeGravitation_GPU_GB300_Newton3": (ctypes.c_float, [c_vp, c_vp, ctypes.c_float,
+                                                              c_size]),
     "nbgb_release_workspace": (None, []),
     "nbgb_force_workspace_bytes": (c_size, [c_size]),
     "nbgb_force": (ctypes.c_int, [c_vp, c_vp, ctypes.c_float, c_size, c_vp, c_size, c_vp]),

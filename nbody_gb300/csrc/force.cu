@@ -878,6 +878,43 @@ done:
     return ms;
 }
 
+// Second table row: the Newton's-third-law variant with the same drop-in
+// conventions (device pointers, legacy stream, ms returned, 0 on error,
+// synchronised); scratch from the same per-device cache.
+NBGB_API float ComputeGravitation_GPU_GB300_Newton3(float *force, float *posMass,
+                                                    float softeningSquared, size_t N) {
+    float ms = 0.0f;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    void *ws = nullptr;
+    size_t bytes = 0;
+    if (N == 0 || !force || !posMass)
+        return 0.0f;
+    bytes = nbgb_force_newton3_workspace_bytes(N);
+    if (!bytes || !(ws = cached_workspace(bytes)))
+        return 0.0f;
+    if (cudaEventCreate(&ev0) != cudaSuccess || cudaEventCreate(&ev1) != cudaSuccess)
+        goto done;
+    if (cudaEventRecord(ev0, nullptr) != cudaSuccess)
+        goto done;
+    if (nbgb_force_newton3(force, posMass, softeningSquared, N, ws, bytes, nullptr) != NBGB_OK)
+        goto done;
+    if (cudaEventRecord(ev1, nullptr) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
+        goto done;
+    {
+        unsigned bits = 0;
+        if (read_and_clear_status(&bits) != NBGB_OK || bits != 0)
+            goto done;
+    }
+    if (cudaEventElapsedTime(&ms, ev0, ev1) != cudaSuccess)
+        ms = 0.0f;
+done:
+    if (ev1)
+        cudaEventDestroy(ev1);
+    if (ev0)
+        cudaEventDestroy(ev0);
+    return ms;
+}
+
 NBGB_API void nbgb_release_workspace(void) { release_workspaces(); }
 
 NBGB_API int nbgb_last_status(void) {

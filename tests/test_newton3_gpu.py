@@ -76,3 +76,15 @@ def test_resident_system_with_newton3(cuda):
     (p1, v1), (p2, v2) = out
     assert np.abs(p1 - p2).max() <= 1e-9 * np.abs(p1).max()
     assert np.abs(v1 - v2).max() <= 1e-8 * np.abs(v1).max()
+
+
+def test_drop_in_row(cuda):
+    import torch
+    g = golden("ball2048")
+    pm = torch.from_numpy(g["posMass"]).cuda()
+    f = torch.full_like(pm, 3.0)
+    ms = nb.ComputeGravitation_GPU_GB300_Newton3(f, pm, float(g["eps2"]), pm.shape[0])
+    assert ms > 0.0
+    out = f.cpu().numpy()
+    assert O.per_body_rel_error(out, g["force_aos"])[0] <= TOL_VS_REFERENCE
+    assert nb.ComputeGravitation_GPU_GB300_Newton3(f, pm, 1e-4, 0) == 0.0
