@@ -16,5 +16,6 @@
 #define NBGB_STATUS_WAIT_TIMEOUT 0x1u /* a bounded mbarrier wait ran out     */
 #define NBGB_STATUS_QUEUE_TIMEOUT 0x2u /* a bounded work-queue wait ran out  */
 #define NBGB_STATUS_BAD_PLAN 0x4u     /* kernel saw an inconsistent plan     */
+#define NBGB_STATUS_NEGATIVE_MASS 0x8u /* a log-domain plan met a mass < 0   */
 
 #endif

@@ -19,7 +19,11 @@
 //                  ring completing on mbarriers, read back with broadcast
 //                  128-bit shared loads, and evaluated two interactions per
 //                  instruction with the f32x2 FP32 instructions (rsqrt on the
-//                  MUFU pipe).  Every 256 sources the FP32 partial sum is
+//                  MUFU pipe; mode 6 takes every fourth source pair's
+//                  m r^-3 in the log domain, 2^(log2 m - 1.5 log2 r^2), to
+//                  move work from the FMA pipe to the MUFU pipe, whose ex2
+//                  runs at twice the rsqrt rate on sm_103).  Every 256
+//                  sources the FP32 partial sum is
 //                  folded into a per-body compensated (TwoSum) running sum.
 //                  With nsplit > 1 the j-range of an i-block is cut into
 //                  nsplit slices so that the number of units fills the GPU's
@@ -65,8 +69,11 @@ struct ForceParams {
 // ---------------------------------------------------------------------------
 // pack: AOS -> paired j-stream, zero-mass padding, counter reset.
 // ---------------------------------------------------------------------------
+// logm != 0 (mode 6 plans): pairs q with q % 4 == 0 carry log2 of their
+// masses (jstream_log_mass) instead of the masses.
 __global__ void pack_jstream_kernel(const float4 *__restrict__ pm, float4 *__restrict__ js, int n,
-                                    int npad, unsigned *__restrict__ counters, int ncounters) {
+                                    int npad, unsigned *__restrict__ counters, int ncounters,
+                                    int logm) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;  // pair index
     if (q < ncounters)
         counters[q] = 0u;
@@ -75,6 +82,10 @@ __global__ void pack_jstream_kernel(const float4 *__restrict__ pm, float4 *__res
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 b0 = (2 * q < n) ? pm[2 * q] : z;
     float4 b1 = (2 * q + 1 < n) ? pm[2 * q + 1] : z;
+    if (logm && jstream_log_slot(q)) {
+        b0.w = jstream_log_mass(b0.w);
+        b1.w = jstream_log_mass(b1.w);
+    }
     js[2 * q] = make_float4(b0.x, b1.x, b0.y, b1.y);
     js[2 * q + 1] = make_float4(b0.z, b1.z, b0.w, b1.w);
 }
@@ -115,6 +126,8 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     // (TwoSum) sum: at most 256 (128 per f32x2 half), whatever the tile size.
     constexpr int FLUSH = JT < 256 ? JT : 256;
     static_assert(JT % FLUSH == 0, "tiles hold whole flush chunks");
+    static_assert(MODE != 6 || (FLUSH % 8 == 0 && (UNROLL < 4 || UNROLL % 4 == 0)),
+                  "mode 6 steps through whole groups of 4 source pairs");
 
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *ring = reinterpret_cast<float4 *>(smem_raw);
@@ -184,6 +197,7 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     const f2 eps2p = f2_pack(p.eps2, p.eps2);
     const f2 zero2 = f2_pack(0.f, 0.f);
     const f2 one2 = f2_pack(1.f, 1.f);
+    const f2 m15 = f2_pack(-1.5f, -1.5f);
 
     // Ring protocol without CTA-wide barriers: every warp waits for a stage's
     // copy on its mbarrier, reads it, then releases it with an acq_rel add;
@@ -264,6 +278,41 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                     comp_add(hz[k], lz[k], l + h);
                     f2_unpack(ap[k], l, h);
                     comp_add(hp[k], lp[k], l + h);
+                }
+                }
+            } else if constexpr (MODE == 6) {  // f32x2, pair q % 4 == 0 in the log domain
+                f2 ax[K], ay[K], az[K];
+                constexpr int GROUPS = UNROLL >= 4 ? UNROLL / 4 : 1;
+                for (int q0 = 0; q0 < JT / 2; q0 += FLUSH / 2) {
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    ax[k] = ay[k] = az[k] = zero2;
+#pragma unroll GROUPS
+                for (int q = q0; q < q0 + FLUSH / 2; q += 4) {
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const ulonglong2 a = tp[2 * (q + u)];
+                        const ulonglong2 b = tp[2 * (q + u) + 1];
+#pragma unroll
+                        for (int k = 0; k < K; k++) {
+                            if (u == 0)
+                                pair_interact2_log(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p,
+                                                   m15, ax[k], ay[k], az[k]);
+                            else
+                                pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p,
+                                               ax[k], ay[k], az[k]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    float l, h;
+                    f2_unpack(ax[k], l, h);
+                    comp_add(hx[k], lx[k], l + h);
+                    f2_unpack(ay[k], l, h);
+                    comp_add(hy[k], ly[k], l + h);
+                    f2_unpack(az[k], l, h);
+                    comp_add(hz[k], lz[k], l + h);
                 }
                 }
             } else if constexpr (MODE != 0) {  // packed f32x2 (MODE 2: all ops as FMAs)
@@ -427,14 +476,16 @@ struct ForceConfig {
     int warps, k, jt, stages;
     int mode;  // 0 scalar FP32, 1 packed f32x2 (source pairs), 2 as 1 with every
                // op as an FMA, 4 packed f32x2 (target pairs, duplicated sources),
-               // 5 as 1 plus the potential in w
+               // 5 as 1 plus the potential in w, 6 as 1 with every fourth source
+               // pair in the log domain (j-stream with log2 masses there)
     const void *fn;
     const char *name;
 };
 
 // W warps, K targets per thread, JT sources per tile, ST ring stages, mode
 // (0 scalar, 1 f32x2, 2 f32x2 all-FMA, 4 f32x2 target pairs, 5 f32x2 with
-// potential), inner unroll, minimum resident CTAs (register cap).
+// potential, 6 f32x2 with log-domain pairs), inner unroll, minimum resident
+// CTAs (register cap).
 #define NBGB_CFG(W, K, JT, ST, PK, UN, MB, PIPE)                                           \
     {W, K, JT, ST, PK, (const void *)force_kernel<W, K, JT, ST, PK, UN, MB>,               \
      "w" #W "_k" #K "_jt" #JT "_s" #ST "_" PIPE}
@@ -467,6 +518,12 @@ static const ForceConfig kConfigs[] = {
     NBGB_CFG(8, 2, 512, 3, 1, 4, 2, "f32x2"),  // 24: as 10, 512-body tiles
     NBGB_CFG(8, 2, 1024, 2, 1, 4, 2, "f32x2"), // 25: as 10, 1024-body tiles
     NBGB_CFG(8, 2, 128, 6, 1, 4, 2, "f32x2"),  // 26: as 10, 128-body tiles
+    NBGB_CFG(8, 2, 1024, 2, 6, 4, 2, "log4"),  // 27: as 25, log-domain pairs
+    NBGB_CFG(8, 2, 512, 3, 6, 4, 2, "log4"),   // 28: as 24, log-domain pairs
+    NBGB_CFG(8, 2, 256, 4, 6, 4, 2, "log4"),   // 29: as 10, log-domain pairs
+    NBGB_CFG(8, 2, 1024, 2, 6, 8, 2, "log4"),  // 30: as 27, unroll 8
+    NBGB_CFG(8, 4, 512, 3, 6, 4, 2, "log4"),   // 31: as 0, log-domain pairs
+    NBGB_CFG(4, 2, 256, 4, 6, 8, 4, "log4"),   // 32: as 3, log-domain pairs
 };
 static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
 // Relative throughput of each configuration (interactions/s per resident
@@ -476,11 +533,15 @@ static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
 static double g_speed[] = {
     0.943, 0.934, 0.981, 0.970, 0.902, 0.981, 0.955, 0.954, 0.962, 0.973,  // 0-9
     0.990, 0.966, 0.873, 0.936, 0.987, 0.981, 0.981, 0.982, 0.981, 0.928,  // 10-19
-    0.987, 0.951, 0.974, 0.900, 0.997, 1.000, 0.977,                       // 20-26
+    0.987, 0.951, 0.974, 0.900, 0.997, 1.000, 0.977, 1.057, 1.030, 1.026,  // 20-29
+    1.034, 1.009, 1.016,                                                   // 30-32
 };
 static_assert(sizeof(g_speed) / sizeof(g_speed[0]) == sizeof(kConfigs) / sizeof(kConfigs[0]),
               "one speed per configuration");
-static const int kDefaultCandidates[] = {25, 24, 10, 20, 2, 3, 5};
+static const int kDefaultCandidates[] = {27, 28, 29, 30, 31, 32, 25, 24, 10, 20, 2, 3, 5};
+// Candidates without log-domain pairs, for masses that have no logarithm
+// (negative masses).
+static const int kRsqrtCandidates[] = {25, 24, 10, 20, 2, 3, 5};
 
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -532,6 +593,7 @@ static void fill_layout(ForcePlan &pl, size_t n) {
     pl.block_bodies = (int)bi;
     pl.tile_bodies = cf.jt;
     pl.js_vpb = cf.mode == 4 ? 2 : 1;
+    pl.js_log = cf.mode == 6 ? 1 : 0;
     pl.nblocks = (int)((n + bi - 1) / bi);
     pl.ntiles = (int)((n + cf.jt - 1) / cf.jt);
     pl.ni_pad = (size_t)pl.nblocks * bi;
@@ -554,21 +616,11 @@ static void fill_layout(ForcePlan &pl, size_t n) {
 // proportional to tiles x JT x BI x (resident CTAs per SM), i.e. the SM's
 // interaction throughput is assumed equal across configurations.  The chosen
 // plan minimises waves x per-unit time.
-int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
-    if (n == 0 || n > kMaxBodies)
-        return NBGB_ERR_INVALID_ARGUMENT;
+static int plan_force_among(size_t n, const std::vector<int> &cands, int force_nsplit,
+                            ForcePlan &pl) {
     const DeviceInfo *d = device_info();
     if (!d)
         return NBGB_ERR_CUDA;
-    std::vector<int> cands;
-    if (force_config >= 0) {
-        if (force_config >= kNumConfigs)
-            return NBGB_ERR_INVALID_ARGUMENT;
-        cands.push_back(force_config);
-    } else {
-        for (int c : kDefaultCandidates)
-            cands.push_back(c);
-    }
     double best = 1e300;
     int best_c = -1, best_s = 1;
     for (int c : cands) {
@@ -605,6 +657,28 @@ int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
     pl.nsplit = best_s;
     fill_layout(pl, n);
     return NBGB_OK;
+}
+
+int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
+    if (n == 0 || n > kMaxBodies)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    std::vector<int> cands;
+    if (force_config >= 0) {
+        if (force_config >= kNumConfigs)
+            return NBGB_ERR_INVALID_ARGUMENT;
+        cands.push_back(force_config);
+    } else {
+        cands.assign(std::begin(kDefaultCandidates), std::end(kDefaultCandidates));
+    }
+    return plan_force_among(n, cands, force_nsplit, pl);
+}
+
+int plan_force_rsqrt(size_t n, ForcePlan &pl) {
+    if (n == 0 || n > kMaxBodies)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    return plan_force_among(n, std::vector<int>(std::begin(kRsqrtCandidates),
+                                                std::end(kRsqrtCandidates)),
+                            -1, pl);
 }
 
 // The best plan (same cost model as plan_force) whose workspace fits in
@@ -687,7 +761,7 @@ int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cud
                                                                           npad, cnt, ncnt);
     else
         pack_jstream_kernel<<<(work + tb - 1) / tb, tb, 0, stream>>>(posMass, js, (int)pl.n, npad,
-                                                                      cnt, ncnt);
+                                                                      cnt, ncnt, pl.js_log);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
@@ -716,6 +790,8 @@ int read_and_clear_status(unsigned *bits) {
     int rc = read_status_force(bits);
     if (rc == NBGB_OK)
         rc = read_status_ensemble(bits);
+    if (rc == NBGB_OK)
+        rc = read_status_integrate(bits);
     return rc;
 }
 
@@ -854,18 +930,26 @@ NBGB_API float ComputeGravitation_GPU_GB300(float *force, float *posMass, float 
         goto done;
     if (cudaEventRecord(ev0, nullptr) != cudaSuccess)
         goto done;
-    if (launch_pack(pl, (const float4 *)posMass, ws, nullptr) != NBGB_OK)
-        goto done;
-    if (launch_force(pl, (float4 *)force, (const float4 *)posMass, nullptr, softeningSquared, ws,
-                     nullptr) != NBGB_OK)
-        goto done;
-    if (cudaEventRecord(ev1, nullptr) != cudaSuccess)
-        goto done;
-    if (cudaDeviceSynchronize() != cudaSuccess)
-        goto done;
-    {
+    for (int attempt = 0; attempt < 2; attempt++) {
+        if (launch_pack(pl, (const float4 *)posMass, ws, nullptr) != NBGB_OK)
+            goto done;
+        if (launch_force(pl, (float4 *)force, (const float4 *)posMass, nullptr, softeningSquared,
+                         ws, nullptr) != NBGB_OK)
+            goto done;
+        if (cudaEventRecord(ev1, nullptr) != cudaSuccess)
+            goto done;
+        if (cudaDeviceSynchronize() != cudaSuccess)
+            goto done;
         unsigned bits = 0;
-        if (read_and_clear_status(&bits) != NBGB_OK || bits != 0)
+        if (read_and_clear_status(&bits) != NBGB_OK)
+            goto done;
+        if (bits == 0)
+            break;
+        // Negative masses met a log-domain plan: evaluate again with rsqrt
+        // only (the reference's arithmetic accepts any sign).
+        if (bits != NBGB_STATUS_NEGATIVE_MASS || attempt > 0 ||
+            plan_force_rsqrt(N, pl) != NBGB_OK || !(ws = cached_workspace(pl.workspace_bytes)) ||
+            cudaEventRecord(ev0, nullptr) != cudaSuccess)
             goto done;
     }
     if (cudaEventElapsedTime(&ms, ev0, ev1) != cudaSuccess)

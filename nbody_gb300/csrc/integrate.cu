@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "nbgb_device.cuh"
 #include "nbgb_internal.h"
 #include "nbody_gb300.h"
 
@@ -29,9 +30,14 @@ namespace nbgb {
 
 // Thread q owns bodies 2q and 2q+1 (one j-stream pair).
 // j-stream store for bodies 2q, 2q+1 in either layout (vpb 1: source pairs,
-// vpb 2: each source duplicated).
-__device__ __forceinline__ void store_jstream(float4 *__restrict__ js, int vpb, int q, float4 b0,
-                                              float4 b1) {
+// vpb 2: each source duplicated); logm: log2 masses in the pairs that carry
+// them in log-domain plans.
+__device__ __forceinline__ void store_jstream(float4 *__restrict__ js, int vpb, int logm, int q,
+                                              float4 b0, float4 b1) {
+    if (logm && jstream_log_slot(q)) {
+        b0.w = jstream_log_mass(b0.w);
+        b1.w = jstream_log_mass(b1.w);
+    }
     if (vpb == 2) {
         js[4 * q] = make_float4(b0.x, b0.x, b0.y, b0.y);
         js[4 * q + 1] = make_float4(b0.z, b0.z, b0.w, b0.w);
@@ -46,8 +52,8 @@ __device__ __forceinline__ void store_jstream(float4 *__restrict__ js, int vpb, 
 __global__ void integrate_reference_kernel(float4 *__restrict__ pm, float4 *__restrict__ vel,
                                            const float4 *__restrict__ force, float dt,
                                            float damping, int n, float4 *__restrict__ js,
-                                           int js_vpb, int npad, unsigned *__restrict__ counters,
-                                           int ncounters) {
+                                           int js_vpb, int js_log, int npad,
+                                           unsigned *__restrict__ counters, int ncounters) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < ncounters)
         counters[q] = 0u;
@@ -74,7 +80,7 @@ __global__ void integrate_reference_kernel(float4 *__restrict__ pm, float4 *__re
         }
     }
     if (js && 2 * q < npad)
-        store_jstream(js, js_vpb, q, out[0], out[1]);
+        store_jstream(js, js_vpb, js_log, q, out[0], out[1]);
 }
 
 // FP64 kick (v += a * kick_dt) then drift (x += v * drift_dt); either may be
@@ -85,7 +91,7 @@ __global__ void kdk_kernel(double *__restrict__ px, double *__restrict__ py,
                            const float *__restrict__ mass, const float4 *__restrict__ accel,
                            double kick_dt, double drift_dt, int write_pos, int n,
                            float4 *__restrict__ pm, float4 *__restrict__ js, int js_vpb,
-                           int npad, unsigned *__restrict__ counters, int ncounters) {
+                           int js_log, int npad, unsigned *__restrict__ counters, int ncounters) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < ncounters)
         counters[q] = 0u;
@@ -121,32 +127,36 @@ __global__ void kdk_kernel(double *__restrict__ px, double *__restrict__ py,
         }
     }
     if (write_pos && js && 2 * q < npad)
-        store_jstream(js, js_vpb, q, out[0], out[1]);
+        store_jstream(js, js_vpb, js_log, q, out[0], out[1]);
 }
 
 int launch_integrate_reference(float4 *pm, float4 *vel, const float4 *force, float dt,
-                               float damping, size_t n, float4 *js, int js_vpb, int npad,
-                               unsigned *counters, int ncounters, cudaStream_t st) {
+                               float damping, size_t n, float4 *js, int js_vpb, int js_log,
+                               int npad, unsigned *counters, int ncounters, cudaStream_t st) {
     const int pairs = (int)((n + 1) / 2);
     const int work = std::max(std::max(pairs, npad / 2), ncounters);
     const int tb = 256;
     integrate_reference_kernel<<<(work + tb - 1) / tb, tb, 0, st>>>(
-        pm, vel, force, dt, damping, (int)n, js, js_vpb, npad, counters, ncounters);
+        pm, vel, force, dt, damping, (int)n, js, js_vpb, js_log, npad, counters, ncounters);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
 int launch_kdk(double *px, double *py, double *pz, double *vx, double *vy, double *vz,
                const float *mass, const float4 *accel, double kick_dt, double drift_dt,
-               int write_pos, size_t n, float4 *pm, float4 *js, int js_vpb, int npad,
+               int write_pos, size_t n, float4 *pm, float4 *js, int js_vpb, int js_log, int npad,
                unsigned *counters, int ncounters, cudaStream_t st) {
     const int pairs = (int)((n + 1) / 2);
     const int work = std::max(std::max(pairs, npad / 2), ncounters);
     const int tb = 256;
     kdk_kernel<<<(work + tb - 1) / tb, tb, 0, st>>>(px, py, pz, vx, vy, vz, mass, accel, kick_dt,
                                                     drift_dt, write_pos, (int)n, pm, js, js_vpb,
-                                                    npad, counters, ncounters);
+                                                    js_log, npad, counters, ncounters);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
+
+static NBGB_STATUS_READER(read_status_integrate_tu)
+
+int read_status_integrate(unsigned *bits) { return read_status_integrate_tu(bits); }
 
 }  // namespace nbgb
 
@@ -162,7 +172,7 @@ NBGB_API int nbgb_integrate_reference(float *posMass, float *velInvMass, const f
         return NBGB_ERR_INVALID_ARGUMENT;
     return nbgb::launch_integrate_reference((float4 *)posMass, (float4 *)velInvMass,
                                             (const float4 *)force, dt, damping, N, nullptr, 1, 0,
-                                            nullptr, 0, (cudaStream_t)stream);
+                                            0, nullptr, 0, (cudaStream_t)stream);
 }
 
 }  // extern "C"

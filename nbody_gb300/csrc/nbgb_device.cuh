@@ -144,6 +144,61 @@ __device__ __forceinline__ void pair_interact2_fma(f2 sx, f2 sy, f2 sz, f2 sm,
     az = f2_fma(dz, s, az);
 }
 
+// MUFU base-2 exponential and logarithm.
+__device__ __forceinline__ float ex2_mufu(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float lg2_mufu(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// pair_interact2 with the scale m * d2^(-3/2) taken in the log domain:
+// s = 2^(log2 m - 1.5 log2 d2), where the source slot holds lm = log2 m
+// (-inf for a zero mass, giving s = 0).  One packed FMA, two MUFU lg2 and two
+// MUFU ex2 replace two MUFU rsqrt and three packed multiplies.  On sm_103 ex2
+// issues at twice the rsqrt / lg2 rate, so mixing both forms moves work from
+// the FMA pipe (the bound) to the MUFU pipe.
+__device__ __forceinline__ void pair_interact2_log(f2 sx, f2 sy, f2 sz, f2 lm, f2 nx, f2 ny,
+                                                   f2 nz, f2 eps2, f2 m15, f2 &ax, f2 &ay,
+                                                   f2 &az) {
+    f2 dx = f2_add(sx, nx);
+    f2 dy = f2_add(sy, ny);
+    f2 dz = f2_add(sz, nz);
+    f2 d2 = f2_fma(dx, dx, eps2);
+    d2 = f2_fma(dy, dy, d2);
+    d2 = f2_fma(dz, dz, d2);
+    float d2l, d2h;
+    f2_unpack(d2, d2l, d2h);
+    f2 e = f2_fma(f2_pack(lg2_mufu(d2l), lg2_mufu(d2h)), m15, lm);
+    float el, eh;
+    f2_unpack(e, el, eh);
+    f2 s = f2_pack(ex2_mufu(el), ex2_mufu(eh));
+    ax = f2_fma(dx, s, ax);
+    ay = f2_fma(dy, s, ay);
+    az = f2_fma(dz, s, az);
+}
+
+// j-stream pairs that carry log2 masses in log-domain (mode 6) plans: pair q
+// with q % 4 == 0 (tiles hold whole groups of 4 pairs, so the tile-local and
+// the global pair index agree modulo 4).
+__device__ __forceinline__ bool jstream_log_slot(int q) { return (q & 3) == 0; }
+
+// log2 m for those pairs: -inf for m == 0 (the pair then contributes 0, as
+// zero-mass padding must).  A negative (or NaN) mass has no logarithm: NaN is
+// stored, so the forces come out NaN, and NBGB_STATUS_NEGATIVE_MASS is set.
+__device__ __forceinline__ float jstream_log_mass(float m) {
+    if (m > 0.f)
+        return log2f(m);
+    if (m == 0.f)
+        return __int_as_float(0xff800000);  // -inf
+    atomicOr(&g_status, NBGB_STATUS_NEGATIVE_MASS);
+    return __int_as_float(0x7fc00000);  // NaN
+}
+
 // One interaction, scalar FP32 pipe.
 __device__ __forceinline__ void pair_interact1(float sx, float sy, float sz, float sm,
                                                float x, float y, float z, float eps2,

@@ -21,12 +21,16 @@ struct ForcePlan {
     int nblocks = 0;      // i-blocks
     int ntiles = 0;       // j-tiles (the j-stream holds ntiles*JT bodies)
     int js_vpb = 1;       // float4s per body in the j-stream (1 pairs, 2 duplicated)
+    int js_log = 0;       // 1: pairs q % 4 == 0 hold log2 masses (mode 6)
     size_t ni_pad = 0;    // nblocks * BI
     size_t off_js = 0, off_hi = 0, off_lo = 0, off_cnt = 0;
     size_t workspace_bytes = 0;
 };
 
 int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl);
+// As plan_force(n, -1, -1), among configurations without log-domain pairs
+// (for masses < 0, which have no logarithm).
+int plan_force_rsqrt(size_t n, ForcePlan &pl);
 int plan_force_within(size_t n, size_t max_bytes, ForcePlan &pl);
 int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream);
 // jstream == nullptr: use the j-stream inside the workspace.
@@ -34,13 +38,14 @@ int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, cons
                  float eps2, void *workspace, cudaStream_t stream);
 int read_and_clear_status(unsigned *bits);
 int read_status_ensemble(unsigned *bits);
-// js_vpb: j-stream layout of the plan the j-stream is written for.
+int read_status_integrate(unsigned *bits);
+// js_vpb, js_log: j-stream layout of the plan the j-stream is written for.
 int launch_integrate_reference(float4 *pm, float4 *vel, const float4 *force, float dt,
-                               float damping, size_t n, float4 *js, int js_vpb, int npad,
-                               unsigned *counters, int ncounters, cudaStream_t st);
+                               float damping, size_t n, float4 *js, int js_vpb, int js_log,
+                               int npad, unsigned *counters, int ncounters, cudaStream_t st);
 int launch_kdk(double *px, double *py, double *pz, double *vx, double *vy, double *vz,
                const float *mass, const float4 *accel, double kick_dt, double drift_dt,
-               int write_pos, size_t n, float4 *pm, float4 *js, int js_vpb, int npad,
+               int write_pos, size_t n, float4 *pm, float4 *js, int js_vpb, int js_log, int npad,
                unsigned *counters, int ncounters, cudaStream_t st);
 size_t diag_scratch_bytes();
 int launch_diagnostics(int n, const double *x64, const float *mass, const float4 *pm,

@@ -147,9 +147,13 @@ __global__ void __launch_bounds__(256) peak_mix_kernel(float *out, int iters, fl
 // shared memory (which = 8): 2 targets x 4 source pairs per iteration;
 // reported as 20 FLOP per interaction, so it compares with the FP32 peak the
 // way the force kernel's figure does.
+//
+// NLOG > 0: the first NLOG of the NS source pairs use the log-domain form
+// (pair_interact2_log), the rest the rsqrt form (which = 11..16).
+template <int NS, int NLOG>
 __global__ void __launch_bounds__(256, 2) peak_interact_kernel(float *out, int iters, float a,
                                                               float b) {
-    constexpr int KT = 2, NS = 4;
+    constexpr int KT = 2;
     f2 nx[KT], ny[KT], nz[KT], ax[KT], ay[KT], az[KT];
     f2 sx[NS], sy[NS], sz[NS], sm[NS];
     const f2 eps2 = f2_pack(1e-4f, 1e-4f), step = f2_pack(a * 1e-7f, b * 1e-7f);
@@ -166,15 +170,21 @@ __global__ void __launch_bounds__(256, 2) peak_interact_kernel(float *out, int i
         sx[c] = f2_pack(0.1f * c, 0.1f * c + 0.05f);
         sy[c] = f2_pack(-0.1f * c, 0.2f);
         sz[c] = f2_pack(0.3f, 0.01f * c);
-        sm[c] = f2_pack(1e-3f, 2e-3f);
+        sm[c] = c < NLOG ? f2_pack(-9.97f, -8.97f) : f2_pack(1e-3f, 2e-3f);
     }
+    const f2 m15 = f2_pack(-1.5f, -1.5f);
     for (int it = 0; it < iters; it++) {
 #pragma unroll
         for (int c = 0; c < NS; c++) {
 #pragma unroll
-            for (int k = 0; k < KT; k++)
-                pair_interact2(sx[c], sy[c], sz[c], sm[c], nx[k], ny[k], nz[k], eps2, ax[k],
-                               ay[k], az[k]);
+            for (int k = 0; k < KT; k++) {
+                if (c < NLOG)
+                    pair_interact2_log(sx[c], sy[c], sz[c], sm[c], nx[k], ny[k], nz[k], eps2,
+                                       m15, ax[k], ay[k], az[k]);
+                else
+                    pair_interact2(sx[c], sy[c], sz[c], sm[c], nx[k], ny[k], nz[k], eps2,
+                                   ax[k], ay[k], az[k]);
+            }
             sx[c] = f2_add(sx[c], step);
         }
     }
@@ -189,17 +199,38 @@ __global__ void __launch_bounds__(256, 2) peak_interact_kernel(float *out, int i
         out[threadIdx.x] = s;
 }
 
+// MUFU throughput: OP 0 = rsqrt (which = 2), 1 = ex2 (which = 9), 2 = lg2
+// (which = 10), 16 dependent chains per thread.  The ex2 and lg2 chains add
+// a constant after each step to stay at a stable fixed point (2^x - 1.5 at
+// x = -1, log2 x + 2 at x = 4); the scalar adds run on the FMA pipe, which
+// has 8x the MUFU rate, so the MUFU pipe stays the bound.
+template <int OP>
 __global__ void __launch_bounds__(256) peak_mufu_kernel(float *out, int iters) {
-    float x[kChains];
+    float x[kChains], z[kChains];
 #pragma unroll
-    for (int c = 0; c < kChains; c++)
+    for (int c = 0; c < kChains; c++) {
         x[c] = 1.0f + (float)(threadIdx.x + c);
+        z[c] = OP == 1 ? -1.0f + 1e-3f * (float)(c + threadIdx.x % 7) : 4.0f + 1e-3f * (float)c;
+    }
     for (int it = 0; it < iters; it++) {
 #pragma unroll
         for (int u = 0; u < 8; u++)
 #pragma unroll
-            for (int c = 0; c < kChains; c++)
-                asm volatile("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(x[c]));
+            for (int c = 0; c < kChains; c++) {
+                if (OP == 0)
+                    asm volatile("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(x[c]));
+                else if (OP == 1)
+                    asm volatile("ex2.approx.ftz.f32 %0, %0;\n\tadd.ftz.f32 %0, %0, 0fBFC00000;"
+                                 : "+f"(z[c]));
+                else
+                    asm volatile("lg2.approx.ftz.f32 %0, %0;\n\tadd.ftz.f32 %0, %0, 0f40000000;"
+                                 : "+f"(z[c]));
+            }
+    }
+    if (OP != 0) {
+#pragma unroll
+        for (int c = 0; c < kChains; c++)
+            x[c] = z[c];
     }
     float s = 0.f;
 #pragma unroll
@@ -218,10 +249,14 @@ extern "C" {
 //        with three varying operands (FLOP/s), 6 = FFMA2 with one MUFU rsqrt
 //        per six (FLOP/s of the FFMA2s), 7 = FFMA2 and scalar FFMA
 //        interleaved (FLOP/s of both), 8 = the force kernel's pair
-//        interaction on register-resident sources (20 FLOP/interaction).
+//        interaction on register-resident sources (20 FLOP/interaction),
+//        9 = MUFU ex2, 10 = MUFU lg2 (ops/s), 11 / 12 = the pair
+//        interaction with 1 / 2 of every 4 source pairs in the log-domain
+//        form, 13 = 8 source pairs per step, 14..16 = 1..3 of every 8 in the
+//        log-domain form.
 // Result in *rate; *ms = best launch time.  Synchronous.
 NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms_out) {
-    if (which < 0 || which > 8 || iters <= 0 || reps <= 0 || !rate)
+    if (which < 0 || which > 16 || iters <= 0 || reps <= 0 || !rate)
         return NBGB_ERR_INVALID_ARGUMENT;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -243,7 +278,11 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
         else if (which == 1)
             nbgb::peak_ffma2_kernel<<<grid, block>>>(out, iters, 0.999f, 1e-3f);
         else if (which == 2)
-            nbgb::peak_mufu_kernel<<<grid, block>>>(out, iters);
+            nbgb::peak_mufu_kernel<0><<<grid, block>>>(out, iters);
+        else if (which == 9)
+            nbgb::peak_mufu_kernel<1><<<grid, block>>>(out, iters);
+        else if (which == 10)
+            nbgb::peak_mufu_kernel<2><<<grid, block>>>(out, iters);
         else if (which == 3)
             nbgb::peak_f2op_kernel<3><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
         else if (which == 4)
@@ -254,8 +293,20 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
             nbgb::peak_mix_kernel<6><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
         else if (which == 7)
             nbgb::peak_mix_kernel<7><<<grid, block>>>(out, iters, 0.999f, 1e-3f);
+        else if (which == 8)
+            nbgb::peak_interact_kernel<4, 0><<<dim3(sms * 2), block>>>(out, iters / 8, 0.999f, 1e-3f);
+        else if (which == 11)
+            nbgb::peak_interact_kernel<4, 1><<<dim3(sms * 2), block>>>(out, iters / 8, 0.999f, 1e-3f);
+        else if (which == 12)
+            nbgb::peak_interact_kernel<4, 2><<<dim3(sms * 2), block>>>(out, iters / 8, 0.999f, 1e-3f);
+        else if (which == 13)
+            nbgb::peak_interact_kernel<8, 0><<<dim3(sms * 2), block>>>(out, iters / 16, 0.999f, 1e-3f);
+        else if (which == 14)
+            nbgb::peak_interact_kernel<8, 1><<<dim3(sms * 2), block>>>(out, iters / 16, 0.999f, 1e-3f);
+        else if (which == 15)
+            nbgb::peak_interact_kernel<8, 2><<<dim3(sms * 2), block>>>(out, iters / 16, 0.999f, 1e-3f);
         else
-            nbgb::peak_interact_kernel<<<dim3(sms * 2), block>>>(out, iters / 8, 0.999f, 1e-3f);
+            nbgb::peak_interact_kernel<8, 3><<<dim3(sms * 2), block>>>(out, iters / 16, 0.999f, 1e-3f);
         cudaEventRecord(e1, nullptr);
         if (cudaEventSynchronize(e1) != cudaSuccess)
             goto done;
@@ -278,8 +329,10 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
             ops = threads * (double)iters * 8 * 8 * 2 * 4;  // FMAs of the FFMA2s only
         else if (which == 7)
             ops = threads * (double)iters * 8 * 8 * (2 * 4 + 2);  // FFMA2s + FFMAs
-        else if (which == 8)  // 20 FLOP x interactions: sms*2 CTAs, NS x KT x 2 per iteration
-            ops = (double)sms * 2 * block.x * (double)(iters / 8) * 4 * 2 * 2 * 20;
+        else if (which == 8 || which == 11 || which == 12)  // 20 FLOP x interactions:
+            ops = (double)sms * 2 * block.x * (double)(iters / 8) * 4 * 2 * 2 * 20;  // NS*KT*2/it
+        else if (which >= 13)
+            ops = (double)sms * 2 * block.x * (double)(iters / 16) * 8 * 2 * 2 * 20;
         *rate = ops / (best * 1e-3);
         if (ms_out)
             *ms_out = best;

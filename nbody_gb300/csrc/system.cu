@@ -39,6 +39,7 @@ struct nbgb_system {
     double *x64 = nullptr;    // KDK: px,py,pz,vx,vy,vz (6 * n doubles)
     float *mass = nullptr;    // KDK: m
     void *ws = nullptr;
+    size_t ws_bytes = 0;
     bool js_valid = false;     // j-stream in ws matches pm
     bool accel_valid = false;  // KDK: force holds a(x) for the current x
     bool use_graph = true;
@@ -113,16 +114,16 @@ int ref_step_body(nbgb_system *s) {
     if (rc != NBGB_OK)
         return rc;
     return nbgb::launch_integrate_reference(s->pm, s->vel, s->force, s->dt, s->damping, s->n,
-                                            js_of(s), s->plan.js_vpb, npad_of(s), cnt_of(s),
-                                            ncnt_of(s), s->stream);
+                                            js_of(s), s->plan.js_vpb, s->plan.js_log, npad_of(s),
+                                            cnt_of(s), ncnt_of(s), s->stream);
 }
 
 // One fused leapfrog body: v += a*kick; x += v*dt; a = F(x).
 int kdk_body(nbgb_system *s, double kick) {
     int rc = nbgb::launch_kdk(comp(s, 0), comp(s, 1), comp(s, 2), comp(s, 3), comp(s, 4),
                               comp(s, 5), s->mass, s->force, kick, (double)s->dt, 1, s->n, s->pm,
-                              js_of(s), s->plan.js_vpb, npad_of(s), cnt_of(s), ncnt_of(s),
-                              s->stream);
+                              js_of(s), s->plan.js_vpb, s->plan.js_log, npad_of(s), cnt_of(s),
+                              ncnt_of(s), s->stream);
     if (rc != NBGB_OK)
         return rc;
     return timed_force(s);
@@ -131,7 +132,44 @@ int kdk_body(nbgb_system *s, double kick) {
 int half_kick(nbgb_system *s) {
     return nbgb::launch_kdk(comp(s, 0), comp(s, 1), comp(s, 2), comp(s, 3), comp(s, 4), comp(s, 5),
                             s->mass, s->force, 0.5 * (double)s->dt, 0.0, 0, s->n, s->pm, nullptr, 1,
-                            0, nullptr, 0, s->stream);
+                            0, 0, nullptr, 0, s->stream);
+}
+
+// Masses below zero (or NaN) have no logarithm: a system whose plan takes
+// some source pairs in the log domain moves to an rsqrt-only plan (growing
+// its workspace if needed) when such masses are set.  m: n masses, stride
+// floats apart (host memory).
+int fit_plan_to_masses(nbgb_system *s, const float *m, size_t stride) {
+    if (!s->plan.js_log)
+        return NBGB_OK;
+    bool all_nonneg = true;
+    for (size_t i = 0; i < s->n && all_nonneg; i++)
+        all_nonneg = m[i * stride] >= 0.f;
+    if (all_nonneg)
+        return NBGB_OK;
+    nbgb::ForcePlan pl;
+    int rc = nbgb::plan_force_rsqrt(s->n, pl);
+    if (rc != NBGB_OK)
+        return rc;
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    if (pl.workspace_bytes > s->ws_bytes) {
+        void *ws = nullptr;
+        if (cudaMalloc(&ws, pl.workspace_bytes) != cudaSuccess)
+            return NBGB_ERR_NO_MEMORY;
+        cudaFree(s->ws);
+        s->ws = ws;
+        s->ws_bytes = pl.workspace_bytes;
+    }
+    // split counters start at zero
+    if (cudaMemsetAsync(s->ws, 0, s->ws_bytes, s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    s->plan = pl;
+    return NBGB_OK;
 }
 
 int check_device_status() {
@@ -208,6 +246,7 @@ NBGB_API nbgb_system *nbgb_system_create(size_t N, int integrator, float softeni
     ok = ok && cudaMalloc(&s->pm, N * 16) == cudaSuccess;
     ok = ok && cudaMalloc(&s->force, N * 16) == cudaSuccess;
     ok = ok && cudaMalloc(&s->ws, s->plan.workspace_bytes) == cudaSuccess;
+    s->ws_bytes = s->plan.workspace_bytes;
     if (integrator == NBGB_INTEGRATOR_REFERENCE) {
         ok = ok && cudaMalloc(&s->vel, N * 16) == cudaSuccess;
     } else {
@@ -248,6 +287,9 @@ NBGB_API int nbgb_system_set_state(nbgb_system *s, const float *posMass, const f
     if (!s || !posMass || !velInvMass)
         return NBGB_ERR_INVALID_ARGUMENT;
     const size_t n = s->n;
+    int rc = fit_plan_to_masses(s, posMass + 3, 4);
+    if (rc != NBGB_OK)
+        return rc;
     if (cudaMemcpyAsync(s->pm, posMass, n * 16, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
         return NBGB_ERR_CUDA;
     if (s->integrator == NBGB_INTEGRATOR_REFERENCE) {
@@ -282,6 +324,9 @@ NBGB_API int nbgb_system_set_state64(nbgb_system *s, const double *pos3, const d
     if (!s || !pos3 || !vel3 || !mass || s->integrator != NBGB_INTEGRATOR_KDK64)
         return NBGB_ERR_INVALID_ARGUMENT;
     const size_t n = s->n;
+    int rc = fit_plan_to_masses(s, mass, 1);
+    if (rc != NBGB_OK)
+        return rc;
     std::vector<double> h(n * 6);
     std::vector<float> pm(n * 4);
     for (size_t i = 0; i < n; i++) {

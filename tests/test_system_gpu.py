@@ -134,3 +134,24 @@ def test_kdk64_conserves_energy_small(cuda):
     # momentum stays ~0
     assert np.abs((m[:, None] * v1).sum(0)).max() < 1e-6
     s.close()
+
+
+def test_negative_masses_replan_the_system(cuda):
+    """A system whose plan takes some source pairs in the log domain moves to
+    an rsqrt-only plan when masses < 0 are set, and its forces then follow the
+    reference's formula for any sign."""
+    n = 3000
+    pm0, vm0 = nb.ic_uniform_ball(n, 99, 1.0, 0.5, 1.5)
+    pm0 = pm0.copy()
+    pm0[0, 3] = -pm0[0, 3]
+    sysm = nb.System(n, nb.INTEGRATOR_REFERENCE, 1e-4, 0.01, 0.95)
+    sysm.set_state(pm0, vm0)
+    cfg, _ = sysm.plan()
+    assert not nb.force_config_names()[cfg].endswith("log4")
+    p_before, _ = sysm.get_state()
+    sysm.step(1)
+    sysm.synchronize()
+    f = sysm.get_force()
+    ref = O.ieee().forces_aos(p_before, 1e-4)
+    assert O.per_body_rel_error(f, ref)[0] <= TOL_FORCE
+    sysm.close()
