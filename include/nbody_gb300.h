@@ -43,7 +43,10 @@ extern "C" {
  * around its launches; returns 0 on any error, which the reference driver
  * treats as "skip this algorithm" (src/nbody.cu:385-386).  Scratch space is
  * allocated on first use and cached per device (nbgb_release_workspace frees
- * it).  Not re-entrant across host threads on the same device.
+ * it).  Not re-entrant across host threads on the same device.  Masses may
+ * have any sign: when the planner's configuration takes source pairs in the
+ * log domain (below) and meets a negative mass, the call evaluates again with
+ * rsqrt-only arithmetic and times that evaluation.
  */
 NBGB_API float ComputeGravitation_GPU_GB300(float *force, float *posMass, float softeningSquared,
                                             size_t N);
@@ -74,6 +77,12 @@ NBGB_API size_t nbgb_force_workspace_bytes(size_t N);
  * NBGB_OK or a negative NBGB_ERR_* code; device-side failures are reported by
  * nbgb_last_status after the stream is synchronised.  Calls that share a
  * workspace must not overlap on the GPU.
+ *
+ * Masses: the planner's default configurations (names ending in "log4") take
+ * every fourth source pair's m r^-3 as 2^(log2 m - 1.5 log2 r^2), which needs
+ * m >= 0.  A negative (or NaN) mass gives NaN forces and sets
+ * NBGB_STATUS_NEGATIVE_MASS; for signed masses force an rsqrt-only
+ * configuration through nbgb_force_ex.
  */
 NBGB_API int nbgb_force(float *force, const float *posMass, float softeningSquared, size_t N,
                         void *workspace, size_t workspace_bytes, void *stream);
@@ -119,6 +128,7 @@ NBGB_API double nbgb_force_get_speed(int config);
  * the array: calls that overlap on the GPU race.  The first call on a device
  * looks up the array's address (once per device); make it before capturing
  * any stream.  Asynchronous on `stream`; returns NBGB_OK or NBGB_ERR_*.
+ * Masses >= 0, as for nbgb_force with the planner's choice.
  */
 NBGB_API int nbgb_force_static(float *force, const float *posMass, float softeningSquared,
                                size_t N, void *stream);
@@ -154,7 +164,8 @@ typedef struct nbgb_system nbgb_system;
 NBGB_API nbgb_system *nbgb_system_create(size_t N, int integrator, float softeningSquared,
                                          float dt, float damping);
 NBGB_API void nbgb_system_destroy(nbgb_system *sys);
-/* HOST float4 arrays in (posMass, velInvMass). */
+/* HOST float4 arrays in (posMass, velInvMass).  A mass < 0 moves the
+   system onto an rsqrt-only force configuration (see nbgb_force). */
 NBGB_API int nbgb_system_set_state(nbgb_system *sys, const float *posMass,
                                    const float *velInvMass);
 /* KDK only: HOST double[N][3] positions and velocities, float[N] masses. */

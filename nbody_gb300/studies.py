@@ -5,6 +5,13 @@ ensemble against looping the plain kernel.
         [--dt 0.002] [--eps2 1e-4] [--sample 4096] [--every 100] [--seed 262144]
     python -m nbody_gb300.studies batched [--systems 4096] [--steps 100]
         [--dt 0.01] [--eps2 1e-4] [--seed 4096] [--plain-sample 4096]
+    python -m nbody_gb300.studies forms [--n 262144] [--sample 4096]
+
+Forms study: the force of one configuration whose pairs all use rsqrt and of
+one that takes every fourth source pair in the log domain, on a seeded
+Plummer sphere and on a 16,384-body uniform ball (m = 1/N), each against the
+FP64 all-pairs sum on a seeded subsample (the whole ball), with the time per
+evaluation.
 
 Precision study:
 
@@ -24,7 +31,8 @@ import time
 
 import numpy as np
 
-from . import (INTEGRATOR_KDK64, System, force_error_stats, force_f64_host, ic_plummer)
+from . import (INTEGRATOR_KDK64, System, force, force_config_names, force_error_stats,
+               force_f64_host, ic_plummer, ic_uniform_ball)
 
 
 def precision_study(n: int = 262144, steps: int = 1000, dt: float = 0.002, eps2: float = 1e-4,
@@ -172,6 +180,36 @@ def batched_study(n_systems: int = 4096, n_lo: int = 64, n_hi: int = 8192, steps
     }
 
 
+def forms_study(n: int = 262144, sample: int = 4096, eps2: float = 1e-4,
+                configs=(25, 27)) -> dict:
+    import torch
+    names = force_config_names()
+    _, _, pm_plummer, _ = ic_plummer(n, 3)
+    pm_ball, _ = ic_uniform_ball(16384, 16384)
+    out = {}
+    for case, pm_np, k in (("plummer", pm_plummer, min(sample, n)), ("ball16384", pm_ball, 16384)):
+        m = pm_np.shape[0]
+        idx = (np.arange(m) if k >= m else
+               np.sort(np.random.default_rng(7).choice(m, k, replace=False)))
+        ref, _ = force_f64_host(pm_np, eps2, idx)
+        pm = torch.from_numpy(pm_np).cuda()
+        rows = {}
+        for c in configs:
+            f = force(pm, eps2, config=c)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(3):
+                force(pm, eps2, out=f, config=c)
+            e1.record()
+            torch.cuda.synchronize()
+            mx, rms = force_error_stats(f.cpu().numpy(), ref, idx)
+            rows[names[c]] = {"max_rel_err_vs_fp64": mx, "rms_rel_err_vs_fp64": rms,
+                              "ms": e0.elapsed_time(e1) / 3}
+        out[case] = {"n": m, "targets_checked": len(idx), "configs": rows}
+    return out
+
+
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="study", required=True)
@@ -192,8 +230,13 @@ def main(argv=None) -> None:
     ba.add_argument("--eps2", type=float, default=1e-4)
     ba.add_argument("--seed", type=int, default=4096)
     ba.add_argument("--plain-sample", type=int, default=4096)
+    fo = sub.add_parser("forms")
+    fo.add_argument("--n", type=int, default=262144)
+    fo.add_argument("--sample", type=int, default=4096)
     a = ap.parse_args(argv)
-    if a.study == "precision":
+    if a.study == "forms":
+        r = forms_study(a.n, a.sample)
+    elif a.study == "precision":
         r = precision_study(a.n, a.steps, a.dt, a.eps2, a.seed, a.sample, a.every)
     else:
         r = batched_study(a.systems, a.n_lo, a.n_hi, a.steps, a.dt, a.eps2, a.seed,
