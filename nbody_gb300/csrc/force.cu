@@ -524,6 +524,9 @@ static const ForceConfig kConfigs[] = {
     NBGB_CFG(8, 2, 1024, 2, 6, 8, 2, "log4"),  // 30: as 27, unroll 8
     NBGB_CFG(8, 4, 512, 3, 6, 4, 2, "log4"),   // 31: as 0, log-domain pairs
     NBGB_CFG(4, 2, 256, 4, 6, 8, 4, "log4"),   // 32: as 3, log-domain pairs
+    NBGB_CFG(8, 3, 1024, 2, 6, 4, 2, "log4"),  // 33: as 27, 3 targets per thread
+    NBGB_CFG(8, 3, 512, 3, 6, 4, 2, "log4"),   // 34: as 28, 3 targets per thread
+    NBGB_CFG(8, 2, 2048, 2, 6, 4, 2, "log4"),  // 35: as 27, 2048-body tiles
 };
 static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
 // Relative throughput of each configuration (interactions/s per resident
@@ -534,7 +537,7 @@ static double g_speed[] = {
     0.943, 0.934, 0.981, 0.970, 0.902, 0.981, 0.955, 0.954, 0.962, 0.973,  // 0-9
     0.990, 0.966, 0.873, 0.936, 0.987, 0.981, 0.981, 0.982, 0.981, 0.928,  // 10-19
     0.987, 0.951, 0.974, 0.900, 0.997, 1.000, 0.977, 1.057, 1.030, 1.026,  // 20-29
-    1.034, 1.009, 1.016,                                                   // 30-32
+    1.034, 1.009, 1.016, 1.000, 1.000, 1.000,                              // 30-35
 };
 static_assert(sizeof(g_speed) / sizeof(g_speed[0]) == sizeof(kConfigs) / sizeof(kConfigs[0]),
               "one speed per configuration");
