@@ -537,7 +537,7 @@ static double g_speed[] = {
     0.943, 0.934, 0.981, 0.970, 0.902, 0.981, 0.955, 0.954, 0.962, 0.973,  // 0-9
     0.990, 0.966, 0.873, 0.936, 0.987, 0.981, 0.981, 0.982, 0.981, 0.928,  // 10-19
     0.987, 0.951, 0.974, 0.900, 0.997, 1.000, 0.977, 1.057, 1.030, 1.026,  // 20-29
-    1.034, 1.009, 1.016, 1.000, 1.000, 1.000,                              // 30-35
+    1.034, 1.009, 1.016, 0.997, 1.020, 1.057,                              // 30-35
 };
 static_assert(sizeof(g_speed) / sizeof(g_speed[0]) == sizeof(kConfigs) / sizeof(kConfigs[0]),
               "one speed per configuration");
