@@ -12,8 +12,10 @@
 //   ens_force        ONE persistent launch: CTAs take work items (system,
 //                    i-block, j-split) from a device queue with an atomic
 //                    counter, largest items first, and evaluate them with the
-//                    same TMA ring, f32x2 pair interaction and TwoSum
-//                    accumulation as the single-system kernel; a system whose
+//                    same TMA ring, f32x2 pair interaction (every fourth
+//                    source pair in the log domain for systems whose masses
+//                    are all >= 0) and TwoSum accumulation as the
+//                    single-system kernel; a system whose
 //                    j-range is split combines its partials in fixed order
 //                    (last item of the i-block, atomic counter)
 //   ens_kick         v += a dt/2 for moving systems
@@ -47,7 +49,9 @@ constexpr int kStages = 3;
 constexpr int kMaxJT = 1024;  // largest tile (bodies); ring stage = 16 KiB
 constexpr uint32_t kStageBytes = kMaxJT * 16u;
 
-enum : int { kMove = 1, kInForce = 2 };
+// kLogMass: j-stream pairs q % 4 == 0 (system-local) hold log2 masses and
+// are evaluated in the log domain (set when every mass is >= 0).
+enum : int { kMove = 1, kInForce = 2, kLogMass = 4 };
 
 // Device descriptor of one system slot.
 struct Desc {
@@ -62,7 +66,7 @@ struct Desc {
     long long part_off;  // into the partial arena (float4 units); lo follows hi
     int cnt_off;         // into the counter arena
     int ni_pad;          // nblocks * block bodies
-    int flags;           // kMove | kInForce
+    int flags;           // kMove | kInForce | kLogMass
     float eps2;
     double dt;
 };
@@ -82,7 +86,7 @@ struct Params {
 // One work item with K targets per thread.  tile_base: tiles this CTA has
 // streamed through its ring before this item (keeps stage phases continuous
 // across items).  Returns false if a bounded wait ran out.
-template <int K, int UNROLL>
+template <int K, int UNROLL, bool LOGM>
 __device__ bool process_item(const Params &P, const Desc &d, int ib, int r, unsigned tile_base,
                              float4 *ring, uint64_t *full, unsigned *released, int *stage_tile,
                              int *abort_flag, int *s_last) {
@@ -121,6 +125,7 @@ __device__ bool process_item(const Params &P, const Desc &d, int ib, int r, unsi
     }
     const f2 eps2p = f2_pack(d.eps2, d.eps2);
     const f2 zero2 = f2_pack(0.f, 0.f);
+    const f2 m15 = f2_pack(-1.5f, -1.5f);
 
     bool failed = false;
     for (int t = 0; t < nt; t++) {
@@ -145,14 +150,35 @@ __device__ bool process_item(const Params &P, const Desc &d, int ib, int r, unsi
 #pragma unroll
             for (int k = 0; k < K; k++)
                 ax[k] = ay[k] = az[k] = zero2;
-#pragma unroll UNROLL
-            for (int q = q0; q < q0 + fpairs; q++) {
-                const ulonglong2 a = tp[2 * q];
-                const ulonglong2 b = tp[2 * q + 1];
+            if constexpr (LOGM) {  // groups of 4 pairs, the first in the log domain
+                constexpr int GROUPS = UNROLL >= 4 ? UNROLL / 4 : 1;
+#pragma unroll GROUPS
+                for (int q = q0; q < q0 + fpairs; q += 4) {
 #pragma unroll
-                for (int k = 0; k < K; k++)
-                    pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p, ax[k],
-                                   ay[k], az[k]);
+                    for (int u = 0; u < 4; u++) {
+                        const ulonglong2 a = tp[2 * (q + u)];
+                        const ulonglong2 b = tp[2 * (q + u) + 1];
+#pragma unroll
+                        for (int k = 0; k < K; k++) {
+                            if (u == 0)
+                                pair_interact2_log(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p,
+                                                   m15, ax[k], ay[k], az[k]);
+                            else
+                                pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p,
+                                               ax[k], ay[k], az[k]);
+                        }
+                    }
+                }
+            } else {
+#pragma unroll UNROLL
+                for (int q = q0; q < q0 + fpairs; q++) {
+                    const ulonglong2 a = tp[2 * q];
+                    const ulonglong2 b = tp[2 * q + 1];
+#pragma unroll
+                    for (int k = 0; k < K; k++)
+                        pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p, ax[k],
+                                       ay[k], az[k]);
+                }
             }
 #pragma unroll
             for (int k = 0; k < K; k++) {
@@ -269,24 +295,27 @@ __global__ void __launch_bounds__(kThreads, 2) ens_force_kernel(Params P) {
             break;
         const int4 item = P.items[it];
         const Desc d = P.desc[item.x];
+        const bool lg = (d.flags & kLogMass) != 0;
+#define NBGB_ENS_ITEM(K, U)                                                                \
+    (lg ? process_item<K, U, true>(P, d, item.y, item.z, tile_base, ring, full, released,  \
+                                   stage_tile, &abort_flag, &s_last)                       \
+        : process_item<K, U, false>(P, d, item.y, item.z, tile_base, ring, full, released, \
+                                    stage_tile, &abort_flag, &s_last))
         switch (d.variant) {
         case 0:
-            ok = process_item<1, 8>(P, d, item.y, item.z, tile_base, ring, full, released,
-                                    stage_tile, &abort_flag, &s_last);
+            ok = NBGB_ENS_ITEM(1, 8);
             break;
         case 1:
-            ok = process_item<2, 4>(P, d, item.y, item.z, tile_base, ring, full, released,
-                                    stage_tile, &abort_flag, &s_last);
+            ok = NBGB_ENS_ITEM(2, 4);
             break;
         case 2:
-            ok = process_item<1, 4>(P, d, item.y, item.z, tile_base, ring, full, released,
-                                    stage_tile, &abort_flag, &s_last);
+            ok = NBGB_ENS_ITEM(1, 4);
             break;
         default:
-            ok = process_item<2, 8>(P, d, item.y, item.z, tile_base, ring, full, released,
-                                    stage_tile, &abort_flag, &s_last);
+            ok = NBGB_ENS_ITEM(2, 8);
             break;
         }
+#undef NBGB_ENS_ITEM
         if (!ok)
             break;
         const int t_begin = (int)(((long long)item.z * d.ntiles) / d.nsplit);
@@ -351,6 +380,10 @@ __global__ void ens_kdk_kernel(const Desc *__restrict__ desc, const int *__restr
         }
     }
     if (mode == 0) {
+        if ((d.flags & kLogMass) && (lp & 3) == 0) {  // log-domain pair (padding: -inf)
+            out[0].w = jstream_log_mass(out[0].w);
+            out[1].w = jstream_log_mass(out[1].w);
+        }
         js[2 * q] = make_float4(out[0].x, out[1].x, out[0].y, out[1].y);
         js[2 * q + 1] = make_float4(out[0].z, out[1].z, out[0].w, out[1].w);
     }
@@ -439,6 +472,7 @@ struct HostSys {
     long long steps_left = 0;
     bool started = false;  // has initial accelerations
     long long steps_done = 0;
+    bool log_mass = false;  // every mass >= 0: log-domain pairs (kLogMass)
 };
 
 // Per-N-bucket plan: bucket b covers N in [2^b, 2^(b+1)).
@@ -523,7 +557,8 @@ void fill_desc(nbgb_ensemble *e, int slot, Desc &d) {
     d.part_off = (long long)h.part_off;
     d.cnt_off = (int)h.cnt_off;
     d.ni_pad = h.ni_pad;
-    d.flags = h.used ? (nbgb::ens::kInForce | (h.started && h.steps_left > 0 ? nbgb::ens::kMove : 0))
+    d.flags = h.used ? (nbgb::ens::kInForce | (h.started && h.steps_left > 0 ? nbgb::ens::kMove : 0) |
+                        (h.log_mass ? nbgb::ens::kLogMass : 0))
                      : 0;
     d.eps2 = e->eps2;
     d.dt = h.dt;
@@ -791,6 +826,9 @@ NBGB_API int nbgb_ensemble_add(nbgb_ensemble *e, const double *pos3, const doubl
     h.dt = dt;
     h.steps_left = steps;
     h.used = true;
+    h.log_mass = true;
+    for (size_t i = 0; i < n && h.log_mass; i++)
+        h.log_mass = mass[i] >= 0.f;
     // upload state (SoA FP64, masses), zero the j-stream range
     std::vector<double> tmp(n);
     cudaStream_t st = e->stream;

@@ -28,7 +28,8 @@ def _f64(pm):
 
 
 @pytest.mark.parametrize("variant,jt,nsplit", [(0, 128, 1), (1, 256, 1), (1, 512, 3),
-                                               (0, 1024, 2), (1, 1024, 1), (-1, 256, 1)])
+                                               (0, 1024, 2), (1, 1024, 1), (-1, 256, 1),
+                                               (0, 16, 1), (3, 32, 2)])
 def test_initial_forces_match_fp64(cuda, variant, jt, nsplit):
     e = nb.Ensemble(60000, 16, EPS2)
     for b in range(32):
@@ -146,3 +147,27 @@ def test_energy_conserved_in_ensemble(cuda):
 
     e0, e1 = energy(p, v), energy(p1, v1)
     assert abs(e1 - e0) / abs(e0) < 1e-4
+
+
+def test_signed_masses_use_rsqrt_pairs(cuda):
+    """A system with a negative mass has no log2 masses: the ensemble keeps it
+    on rsqrt-only pairs (no status bit, finite forces), and its first forces
+    match FP64 like any other system's; its neighbours keep log-domain pairs."""
+    e = nb.Ensemble(20000, 4, EPS2)
+    p, v, m, pm = _ball(3000, 71)
+    m = m.copy()
+    m[0] = -m[0]
+    m[1500] = -0.5 * m[1500]
+    pm = pm.copy()
+    pm[:, 3] = m
+    p2, v2, m2, pm2 = _ball(2000, 72)
+    a_slot = e.add(p, v, m, 0.01, 3)
+    b_slot = e.add(p2, v2, m2, 0.01, 3)
+    e.tick(1)
+    e.synchronize()
+    assert nb.last_status() == 0
+    for slot, ref_pm in ((a_slot, pm), (b_slot, pm2)):
+        _, _, a = e.get_state(slot)
+        assert np.all(np.isfinite(a))
+        assert O.per_body_rel_error(a, _f64(ref_pm))[0] <= TOL_VS_FP64
+    e.close()
