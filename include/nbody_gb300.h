@@ -236,6 +236,12 @@ NBGB_API int nbgb_ensemble_get_state(nbgb_ensemble *ens, int slot, double *pos3,
                                      float *acc4);
 /* info[6]: bodies, steps done, steps left, variant, tile, j-split. */
 NBGB_API int nbgb_ensemble_slot_info(nbgb_ensemble *ens, int slot, long long *info6);
+/* Steps a system takes per tick, 1..8 (default 1), from the next tick on: a
+   tick runs up to 8 passes, pass p moving the systems whose sub exceeds p, so
+   small systems advance several steps while large ones advance one.  Each
+   step is the same KDK step of size dt, so results do not depend on sub.  A
+   system with s steps then finishes after 1 + ceil(s / sub) ticks. */
+NBGB_API int nbgb_ensemble_set_substeps(nbgb_ensemble *ens, int slot, int sub);
 NBGB_API int nbgb_ensemble_remove(nbgb_ensemble *ens, int slot);
 NBGB_API int nbgb_ensemble_active(nbgb_ensemble *ens);
 NBGB_API void *nbgb_ensemble_stream(nbgb_ensemble *ens);

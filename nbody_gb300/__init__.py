@@ -365,6 +365,11 @@ class Ensemble:
         return {"n": int(info[0]), "steps_done": int(info[1]), "steps_left": int(info[2]),
                 "variant": int(info[3]), "jt": int(info[4]), "nsplit": int(info[5])}
 
+    def set_substeps(self, slot: int, sub: int):
+        """Steps this system takes per tick (1..8) from the next tick on; it
+        then finishes after 1 + ceil(steps / sub) ticks."""
+        check(self.lib.nbgb_ensemble_set_substeps(self.h, slot, sub), "ensemble_set_substeps")
+
     def remove(self, slot: int):
         check(self.lib.nbgb_ensemble_remove(self.h, slot), "ensemble_remove")
         self._n.pop(slot, None)

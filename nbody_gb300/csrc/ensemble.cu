@@ -20,9 +20,16 @@
 //                    (last item of the i-block, atomic counter)
 //   ens_kick         v += a dt/2 for moving systems
 //
+// Sub-cycling: a system may take up to kMaxSub steps per tick (its `sub`).
+// A tick then runs passes p = 0 .. max sub - 1, each the three launches above
+// over the systems whose effective sub (min(sub, steps left)) exceeds p, so
+// small systems advance several steps while large ones advance one.  Pass p's
+// work items are a suffix of one list sorted by effective sub (ascending),
+// then cost (descending).
+//
 // A system's decomposition (kernel variant, tile size, j-split) depends only
 // on its own N, so its result is bit-identical whether it runs alone or in
-// any mix.  Newly admitted systems spend their first tick in the force pass
+// any mix (with any sub).  Newly admitted systems spend their first tick in the force pass
 // only (their initial accelerations); systems whose steps are done leave the
 // tick.  While the membership is unchanged the tick is replayed from a CUDA
 // graph.  Admission is bounded by a slot count and a device-memory budget.
@@ -52,6 +59,7 @@ constexpr uint32_t kStageBytes = kMaxJT * 16u;
 // kLogMass: j-stream pairs q % 4 == 0 (system-local) hold log2 masses and
 // are evaluated in the log domain (set when every mass is >= 0).
 enum : int { kMove = 1, kInForce = 2, kLogMass = 4 };
+constexpr int kMaxSub = 8;  // steps per tick of one system, at most
 
 // Device descriptor of one system slot.
 struct Desc {
@@ -67,6 +75,7 @@ struct Desc {
     int cnt_off;         // into the counter arena
     int ni_pad;          // nblocks * block bodies
     int flags;           // kMove | kInForce | kLogMass
+    int sub;             // passes of this tick the system moves in (1..kMaxSub)
     float eps2;
     double dt;
 };
@@ -331,11 +340,13 @@ __global__ void __launch_bounds__(kThreads, 2) ens_force_kernel(Params P) {
 
 // Thread q owns j-stream pair slot q (bodies 2p, 2p+1 of system slot_sys[q]).
 // mode 0: kick half + drift for moving systems, then write posMass and the
-// j-stream of every active system; mode 1: kick half only.
+// j-stream of every active system; mode 1: kick half only.  pass > 0: only
+// moving systems with sub > pass take part.
 __global__ void ens_kdk_kernel(const Desc *__restrict__ desc, const int *__restrict__ slot_sys,
                                int n_slots, double *__restrict__ x64, size_t stride,
                                const float *__restrict__ mass, const float4 *__restrict__ acc,
-                               float4 *__restrict__ pm, float4 *__restrict__ js, int mode) {
+                               float4 *__restrict__ pm, float4 *__restrict__ js, int mode,
+                               int pass) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n_slots)
         return;
@@ -344,6 +355,8 @@ __global__ void ens_kdk_kernel(const Desc *__restrict__ desc, const int *__restr
         return;
     const Desc d = desc[sys];
     if (!(d.flags & kInForce))
+        return;
+    if (pass > 0 && (!(d.flags & kMove) || d.sub <= pass))
         return;
     const bool move = (d.flags & kMove) != 0;
     const int lp = q - d.js_off / 2;
@@ -473,7 +486,15 @@ struct HostSys {
     bool started = false;  // has initial accelerations
     long long steps_done = 0;
     bool log_mass = false;  // every mass >= 0: log-domain pairs (kLogMass)
+    int sub = 1;            // steps per tick (1..kMaxSub)
 };
+
+// Steps a system takes in the coming tick (0 before its initial forces).
+inline int sub_eff(const HostSys &h) {
+    if (!h.started)
+        return 1;  // the initial-force pass
+    return (int)std::min<long long>(h.sub, h.steps_left);
+}
 
 // Per-N-bucket plan: bucket b covers N in [2^b, 2^(b+1)).
 struct BucketPlan {
@@ -506,6 +527,8 @@ struct nbgb_ensemble {
     RangeAlloc a_body, a_js, a_part, a_cnt;
     BucketPlan bucket[32];
     int n_items = 0, n_slots = 0;
+    int n_pass = 1;                       // passes per tick (max effective sub)
+    int pass_first[nbgb::ens::kMaxSub];   // first item of pass p (items sorted by sub)
     bool dirty = true;
     cudaGraphExec_t graph = nullptr;
     bool use_graph = true;
@@ -560,6 +583,7 @@ void fill_desc(nbgb_ensemble *e, int slot, Desc &d) {
     d.flags = h.used ? (nbgb::ens::kInForce | (h.started && h.steps_left > 0 ? nbgb::ens::kMove : 0) |
                         (h.log_mass ? nbgb::ens::kLogMass : 0))
                      : 0;
+    d.sub = h.used ? sub_eff(h) : 1;
     d.eps2 = e->eps2;
     d.dt = h.dt;
 }
@@ -573,6 +597,7 @@ int rebuild(nbgb_ensemble *e) {
     struct It {
         int4 v;
         double cost;
+        int sub;
     };
     std::vector<It> items;
     for (int s = 0; s < e->max_systems; s++) {
@@ -591,16 +616,28 @@ int rebuild(nbgb_ensemble *e) {
                 const int tb = (int)(((long long)r * h.ntiles) / h.nsplit);
                 const int te = (int)(((long long)(r + 1) * h.ntiles) / h.nsplit);
                 items.push_back(It{make_int4(s, b, r, 0),
-                                   (double)(te - tb) * h.jt * bi + 4096.0});
+                                   (double)(te - tb) * h.jt * bi + 4096.0, sub_eff(h)});
             }
     }
-    std::stable_sort(items.begin(), items.end(),
-                     [](const It &a, const It &b) { return a.cost > b.cost; });
+    // by effective sub (ascending), then largest first: pass p's items are
+    // the suffix of systems with sub > p
+    std::stable_sort(items.begin(), items.end(), [](const It &a, const It &b) {
+        return a.sub != b.sub ? a.sub < b.sub : a.cost > b.cost;
+    });
     if (items.size() > e->items_cap)
         return NBGB_ERR_NO_MEMORY;
     for (size_t k = 0; k < items.size(); k++)
         e->h_items[k] = items[k].v;
     e->n_items = (int)items.size();
+    e->n_pass = 1;
+    for (const It &it : items)
+        e->n_pass = std::max(e->n_pass, it.sub);
+    for (int p = 0; p < nbgb::ens::kMaxSub; p++) {
+        int k = 0;
+        while (k < e->n_items && items[k].sub <= p)
+            k++;
+        e->pass_first[p] = p == 0 ? 0 : k;
+    }
     // slot map over the used part of the j-stream arena (pairs)
     size_t end = 0;
     for (int s = 0; s < e->max_systems; s++)
@@ -637,25 +674,33 @@ int launch_tick(nbgb_ensemble *e) {
     cudaStream_t st = e->stream;
     const int tb = 256;
     const int nb = std::max(1, (e->n_slots + tb - 1) / tb);
-    nbgb::ens::ens_kdk_kernel<<<nb, tb, 0, st>>>(e->d_desc, e->d_slot_sys, e->n_slots, e->x64,
-                                                 e->max_bodies, e->mass, e->acc, e->pm, e->js, 0);
-    if (cudaMemsetAsync(e->head, 0, sizeof(unsigned), st) != cudaSuccess)
-        return NBGB_ERR_CUDA;
-    nbgb::ens::Params P;
-    P.desc = e->d_desc;
-    P.items = e->d_items;
-    P.n_items = e->n_items;
-    P.head = e->head;
-    P.pm = e->pm;
-    P.js = e->js;
-    P.acc = e->acc;
-    P.part = e->part;
-    P.cnt = e->cnt;
-    if (e->n_items > 0)
-        nbgb::ens::ens_force_kernel<<<e->grid, nbgb::ens::kThreads,
-                                      nbgb::ens::kStages * nbgb::ens::kStageBytes, st>>>(P);
-    nbgb::ens::ens_kdk_kernel<<<nb, tb, 0, st>>>(e->d_desc, e->d_slot_sys, e->n_slots, e->x64,
-                                                 e->max_bodies, e->mass, e->acc, e->pm, e->js, 1);
+    for (int pass = 0; pass < e->n_pass; pass++) {
+        const int first = e->pass_first[pass];
+        const int n_items = e->n_items - first;
+        if (pass > 0 && n_items <= 0)
+            break;
+        nbgb::ens::ens_kdk_kernel<<<nb, tb, 0, st>>>(e->d_desc, e->d_slot_sys, e->n_slots,
+                                                     e->x64, e->max_bodies, e->mass, e->acc,
+                                                     e->pm, e->js, 0, pass);
+        if (cudaMemsetAsync(e->head, 0, sizeof(unsigned), st) != cudaSuccess)
+            return NBGB_ERR_CUDA;
+        nbgb::ens::Params P;
+        P.desc = e->d_desc;
+        P.items = e->d_items + first;
+        P.n_items = n_items;
+        P.head = e->head;
+        P.pm = e->pm;
+        P.js = e->js;
+        P.acc = e->acc;
+        P.part = e->part;
+        P.cnt = e->cnt;
+        if (n_items > 0)
+            nbgb::ens::ens_force_kernel<<<e->grid, nbgb::ens::kThreads,
+                                          nbgb::ens::kStages * nbgb::ens::kStageBytes, st>>>(P);
+        nbgb::ens::ens_kdk_kernel<<<nb, tb, 0, st>>>(e->d_desc, e->d_slot_sys, e->n_slots,
+                                                     e->x64, e->max_bodies, e->mass, e->acc,
+                                                     e->pm, e->js, 1, pass);
+    }
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
@@ -901,10 +946,11 @@ NBGB_API int nbgb_ensemble_tick(nbgb_ensemble *e, int nticks) {
                 h.started = true;
                 e->dirty = true;  // moves from the next tick on
             } else if (h.steps_left > 0) {
-                h.steps_left--;
-                h.steps_done++;
-                if (h.steps_left == 0)
-                    e->dirty = true;  // leaves the tick
+                const int k = sub_eff(h);
+                h.steps_left -= k;
+                h.steps_done += k;
+                if (h.steps_left < h.sub)
+                    e->dirty = true;  // leaves the tick, or fewer steps next tick
             }
         }
     }
@@ -979,6 +1025,18 @@ NBGB_API int nbgb_ensemble_slot_info(nbgb_ensemble *e, int slot, long long *info
     info6[3] = h.variant;
     info6[4] = h.jt;
     info6[5] = h.nsplit;
+    return NBGB_OK;
+}
+
+// Steps per tick of one system (1..8); takes effect from the next tick.
+NBGB_API int nbgb_ensemble_set_substeps(nbgb_ensemble *e, int slot, int sub) {
+    if (!e || slot < 0 || slot >= e->max_systems || !e->sys[slot].used || sub < 1 ||
+        sub > nbgb::ens::kMaxSub)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (e->sys[slot].sub != sub) {
+        e->sys[slot].sub = sub;
+        e->dirty = true;
+    }
     return NBGB_OK;
 }
 

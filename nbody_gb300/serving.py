@@ -3,7 +3,7 @@
     python -m nbody_gb300.serving [--requests 20000] [--rates 10,inf] [--seed 5]
         [--n-lo 256] [--n-hi 65536] [--steps-lo 10] [--steps-hi 1000]
         [--dt 0.005] [--eps2 1e-4] [--budget-gb 120] [--slots 512]
-        [--plain-sample N]
+        [--plain-sample N] [--work-budgets 2e10,1e10]
 
 Requests arrive as a Poisson process (rate per second; inf = all at t = 0),
 each with N log-uniform in [n_lo, n_hi], steps uniform in [steps_lo,
@@ -199,8 +199,8 @@ def _pct(x, q):
     return float(np.percentile(np.asarray(x), q)) if len(x) else None
 
 
-def _batched_run(reqs, eps2, dt, budget_gb, slots):
-    srv = BatchedServer(eps2, dt, budget_gb * 1e9, slots)
+def _batched_run(reqs, eps2, dt, budget_gb, slots, work_budget=2e10):
+    srv = BatchedServer(eps2, dt, budget_gb * 1e9, slots, work_budget=work_budget)
     recs, _, info = srv.run(reqs)
     srv.close()
     lat = [r["latency"] for r in recs.values() if "latency" in r]
@@ -211,16 +211,19 @@ def _batched_run(reqs, eps2, dt, budget_gb, slots):
             "tick_loop_s": info["host_and_gpu_tick_s"], "systems_per_s": len(lat) / span,
             "interactions_per_s": inter / span, "latency_p50_s": _pct(lat, 50),
             "latency_p99_s": _pct(lat, 99),
-            "latency_mean_s": float(np.mean(lat)) if lat else None}
+            "latency_mean_s": float(np.mean(lat)) if lat else None,
+            "work_budget": work_budget}
 
 
 def serve_study(n_req: int = 20000, rates=(10.0,), seed: int = 5, n_lo: int = 256,
                 n_hi: int = 65536, steps_lo: int = 10, steps_hi: int = 1000, dt: float = 0.005,
                 eps2: float = 1e-4, budget_gb: float = 120.0, slots: int = 512,
-                plain_sample: int | None = None) -> dict:
+                plain_sample: int | None = None, work_budgets=(2e10,)) -> dict:
     """Both servers on the same stream at each arrival rate.  The plain
     server's per-request service times are measured once (they do not depend
-    on the arrival times) and replayed through the FIFO rule at every rate."""
+    on the arrival times) and replayed through the FIFO rule at every rate.
+    The batched server runs once per work budget (interactions per tick
+    above which large requests wait); the first budget is the headline."""
     base = make_requests(n_req, 1.0, seed, n_lo, n_hi, steps_lo, steps_hi)
     rng = np.random.default_rng(seed + 17)
     if plain_sample is None or plain_sample >= n_req:
@@ -246,15 +249,19 @@ def serve_study(n_req: int = 20000, rates=(10.0,), seed: int = 5, n_lo: int = 25
            "plain_service_predicted": len(measured) != n_req, "by_rate": []}
     for rate in rates:
         reqs = make_requests(n_req, rate, seed, n_lo, n_hi, steps_lo, steps_hi)
-        b = _batched_run(reqs, eps2, dt, budget_gb, slots)
+        runs = [_batched_run(reqs, eps2, dt, budget_gb, slots, wb) for wb in work_budgets]
+        b = runs[0]
         arrivals = [r["arrival"] for r in reqs]
         pfin = fifo_finish_times(arrivals, service)
         plat = [f - a for f, a in zip(pfin, arrivals)]
         pspan = pfin[-1] - arrivals[0]
         p = {"systems_per_s": n_req / pspan, "latency_p50_s": _pct(plat, 50),
              "latency_p99_s": _pct(plat, 99), "latency_mean_s": float(np.mean(plat))}
-        out["by_rate"].append({"rate_per_s": rate, "batched": b, "plain": p,
-                               "speedup_systems_per_s": b["systems_per_s"] / p["systems_per_s"]})
+        row = {"rate_per_s": rate, "batched": b, "plain": p,
+               "speedup_systems_per_s": b["systems_per_s"] / p["systems_per_s"]}
+        if len(runs) > 1:
+            row["batched_other_work_budgets"] = runs[1:]
+        out["by_rate"].append(row)
     return out
 
 
@@ -273,10 +280,15 @@ def main(argv=None):
     ap.add_argument("--budget-gb", type=float, default=120.0)
     ap.add_argument("--slots", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=None)
+    ap.add_argument("--work-budgets", default="2e10",
+                    help="comma-separated interactions per tick above which large requests "
+                         "wait; the batched server runs once per value, the first is the "
+                         "headline")
     a = ap.parse_args(argv)
     rates = [float(x) for x in a.rates.split(",")]
+    budgets = [float(x) for x in a.work_budgets.split(",")]
     r = serve_study(a.requests, rates, a.seed, a.n_lo, a.n_hi, a.steps_lo, a.steps_hi, a.dt,
-                    a.eps2, a.budget_gb, a.slots, a.plain_sample)
+                    a.eps2, a.budget_gb, a.slots, a.plain_sample, budgets)
     print(json.dumps(r))
 
 

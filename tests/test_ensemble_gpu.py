@@ -171,3 +171,46 @@ def test_signed_masses_use_rsqrt_pairs(cuda):
         assert np.all(np.isfinite(a))
         assert O.per_body_rel_error(a, _f64(ref_pm))[0] <= TOL_VS_FP64
     e.close()
+
+
+def test_substeps_give_identical_results_and_fewer_ticks(cuda):
+    """Sub-cycling: a system taking `sub` steps per tick does exactly the
+    same KDK steps, so its final state is bit-identical to the one-step-per-
+    tick run alone, whatever the mix; it finishes after 1 + ceil(steps/sub)
+    ticks."""
+    dt = 0.002
+    cases = [(300, 13, 4), (1500, 9, 8), (4100, 7, 1), (700, 10, 3)]  # n, steps, sub
+
+    def alone(n, steps):
+        p, v, m, _ = _ball(n, n)
+        e = nb.Ensemble(10000, 2, EPS2)
+        s = e.add(p, v, m, dt, steps)
+        e.tick(steps + 1)
+        e.synchronize()
+        assert e.finished() == [s]
+        out = e.get_state(s)
+        e.close()
+        return out
+
+    ref = {n: alone(n, steps) for n, steps, _ in cases}
+    e = nb.Ensemble(40000, 8, EPS2)
+    slots = {}
+    for n, steps, sub in cases:
+        p, v, m, _ = _ball(n, n)
+        slots[n] = e.add(p, v, m, dt, steps)
+        e.set_substeps(slots[n], sub)
+    done_at, t = {}, 0
+    while len(done_at) < len(cases) and t < 50:
+        e.tick(1)
+        t += 1
+        for s in e.finished():
+            n = next(k for k, v in slots.items() if v == s)
+            if n not in done_at:
+                done_at[n] = t
+                got = e.get_state(s)
+                for a, b in zip(got, ref[n]):
+                    assert np.array_equal(a, b), n
+                e.remove(s)
+    e.close()
+    for n, steps, sub in cases:
+        assert done_at[n] == 1 + -(-steps // sub), (n, done_at[n])
