@@ -242,6 +242,11 @@ NBGB_API int nbgb_ensemble_slot_info(nbgb_ensemble *ens, int slot, long long *in
    step is the same KDK step of size dt, so results do not depend on sub.  A
    system with s steps then finishes after 1 + ceil(s / sub) ticks. */
 NBGB_API int nbgb_ensemble_set_substeps(nbgb_ensemble *ens, int slot, int sub);
+/* CTAs of the persistent force launch, 1..nbgb_ensemble_max_grid (SMs x
+   resident CTAs per SM; 0 = all, the default).  Two ensembles whose grids
+   together fit the resident slots run side by side on their own streams. */
+NBGB_API int nbgb_ensemble_set_grid(nbgb_ensemble *ens, int ctas);
+NBGB_API int nbgb_ensemble_max_grid(nbgb_ensemble *ens);
 NBGB_API int nbgb_ensemble_remove(nbgb_ensemble *ens, int slot);
 NBGB_API int nbgb_ensemble_active(nbgb_ensemble *ens);
 NBGB_API void *nbgb_ensemble_stream(nbgb_ensemble *ens);

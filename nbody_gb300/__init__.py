@@ -370,6 +370,13 @@ class Ensemble:
         then finishes after 1 + ceil(steps / sub) ticks."""
         check(self.lib.nbgb_ensemble_set_substeps(self.h, slot, sub), "ensemble_set_substeps")
 
+    def set_grid(self, ctas: int):
+        """CTAs of the persistent force launch (0 = all resident slots)."""
+        check(self.lib.nbgb_ensemble_set_grid(self.h, ctas), "ensemble_set_grid")
+
+    def max_grid(self) -> int:
+        return int(self.lib.nbgb_ensemble_max_grid(self.h))
+
     def remove(self, slot: int):
         check(self.lib.nbgb_ensemble_remove(self.h, slot), "ensemble_remove")
         self._n.pop(slot, None)

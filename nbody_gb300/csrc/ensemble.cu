@@ -533,7 +533,8 @@ struct nbgb_ensemble {
     cudaGraphExec_t graph = nullptr;
     bool use_graph = true;
     int stable_ticks = 0;  // ticks since the membership last changed
-    int grid = 0;
+    int grid = 0;      // CTAs of the persistent force launch
+    int grid_max = 0;  // SMs x resident CTAs per SM
     size_t bytes_total = 0;
     long long ticks = 0;
 };
@@ -789,6 +790,7 @@ NBGB_API nbgb_ensemble *nbgb_ensemble_create(size_t max_bodies, int max_systems,
         return nullptr;
     }
     e->grid = sms * occ;
+    e->grid_max = e->grid;
     e->bytes_total = max_bodies * (6 * 8 + 4 + 16 + 16) + e->js_cap * 16 + e->part_cap * 16 +
                      e->cnt_cap * 4;
     return e;
@@ -956,6 +958,26 @@ NBGB_API int nbgb_ensemble_tick(nbgb_ensemble *e, int nticks) {
     }
     return NBGB_OK;
 }
+
+// CTAs of the persistent force launch (1 .. SMs x resident CTAs; 0 = all).
+// Two ensembles on one GPU can run side by side when their grids together
+// fit the GPU's resident CTA slots.
+NBGB_API int nbgb_ensemble_set_grid(nbgb_ensemble *e, int ctas) {
+    if (!e || ctas < 0 || ctas > e->grid_max)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const int g = ctas == 0 ? e->grid_max : ctas;
+    if (g != e->grid) {
+        e->grid = g;
+        if (e->graph) {  // the captured tick launches the old grid
+            cudaGraphExecDestroy(e->graph);
+            e->graph = nullptr;
+        }
+    }
+    return NBGB_OK;
+}
+
+// Resident CTA slots of the persistent force launch on this device.
+NBGB_API int nbgb_ensemble_max_grid(nbgb_ensemble *e) { return e ? e->grid_max : 0; }
 
 NBGB_API int nbgb_ensemble_set_graph(nbgb_ensemble *e, int enable) {
     if (!e)

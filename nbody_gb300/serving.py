@@ -3,7 +3,8 @@
     python -m nbody_gb300.serving [--requests 20000] [--rates 10,inf] [--seed 5]
         [--n-lo 256] [--n-hi 65536] [--steps-lo 10] [--steps-hi 1000]
         [--dt 0.005] [--eps2 1e-4] [--budget-gb 120] [--slots 512]
-        [--plain-sample N] [--work-budgets 2e10,1e10]
+        [--plain-sample N] [--work-budgets 2e10,1e10] [--sub-work 0]
+        [--express-n 8192] [--records PATH]
 
 Requests arrive as a Poisson process (rate per second; inf = all at t = 0),
 each with N log-uniform in [n_lo, n_hi], steps uniform in [steps_lo,
@@ -14,7 +15,9 @@ arrived is admitted at a tick boundary when a slot is free and its device
 state fits the HBM state budget; large requests are admitted first come first
 served while the active work per tick is below a work budget (about what
 saturates the GPU), small requests join at once.  Admitted requests share
-every tick (one persistent force launch for all of them); a request whose
+every tick (one persistent force launch per step level for all of them);
+small requests take up to 8 steps per tick (ensemble sub-cycling), so
+they are not held to the pace of the large ones; a request whose
 steps are done is retired at the tick boundary, its final state is copied
 back, and its slot and memory are freed for the next arrivals.  Latency =
 completion time - arrival time.
@@ -61,35 +64,26 @@ def _initial_state(req):
     return p, v, pm[:, 3].copy()
 
 
-class BatchedServer:
-    """Continuous batching over one ensemble arena."""
+class _Lane:
+    """One ensemble arena with its own stream, admission state and loop."""
 
-    def __init__(self, eps2: float = 1e-4, dt: float = 0.005, budget_bytes: float = 120e9,
-                 max_slots: int = 512, max_bodies: int | None = None,
-                 max_ticks_per_sync: int = 32, work_budget: float = 2e10,
-                 small_work: float = 1e8):
-        """work_budget: interactions per tick above which large requests wait
-        (first come first served) instead of joining -- about what saturates
-        the GPU, so joining would only slow everyone; requests whose own work
-        per tick is below small_work always join (slots and memory allowing)."""
-        from . import Ensemble
+    def __init__(self, ens, budget_bytes, max_slots, dt, max_ticks_per_sync, work_budget,
+                 small_work, sub_work):
+        self.ens = ens
+        self.budget = budget_bytes
+        self.max_slots = max_slots
         self.dt = dt
         self.max_ticks_per_sync = max_ticks_per_sync
         self.work_budget = work_budget
         self.small_work = small_work
-        self.budget = budget_bytes
-        self.max_slots = max_slots
-        if max_bodies is None:
-            max_bodies = int(min(budget_bytes // BYTES_PER_BODY, 32 << 20))
-        self.ens = Ensemble(max_bodies, max_slots, eps2)
+        self.sub_work = sub_work
         self.used_bytes = 0
 
-    def close(self):
-        self.ens.close()
+    def _sub(self, n: int) -> int:
+        return int(max(1, min(8, self.sub_work // (float(n) ** 2))))
 
-    def run(self, requests, keep_states=(), time_limit: float | None = None):
-        """Serve `requests` (dicts with n, steps, seed, arrival) in real time.
-        Returns per-request records and, for ids in keep_states, final states.
+    def serve(self, requests, t0, keep_states=(), time_limit=None):
+        """Serve `requests` (arrival times relative to t0) in real time.
         While a tick runs on the GPU the host prepares the initial states of
         requests that have arrived; admission happens at tick boundaries."""
         ens = self.ens
@@ -97,7 +91,6 @@ class BatchedServer:
         ready = deque()  # arrived, initial state generated, not yet admitted
         running = {}
         records, states = {}, {}
-        t0 = time.perf_counter()
         ticks = 0
         busy_s = 0.0
 
@@ -114,9 +107,12 @@ class BatchedServer:
                 break
             prepare(self.max_slots - len(running) + 8)
             # admission: large requests first come first served while the
-            # active work per tick is below the work budget; small ones always
-            work = sum(float(x["n"]) ** 2 for x in running.values())
+            # large requests' work per step is below the work budget; small
+            # ones always join and do not count against it
+            work = sum(float(x["n"]) ** 2 for x in running.values()
+                       if float(x["n"]) ** 2 > self.small_work)
             k = 0
+            large_blocked = False  # strict FCFS among large requests
             while k < len(ready):
                 r, (p, v, m) = ready[k]
                 w = float(r["n"]) ** 2
@@ -124,24 +120,32 @@ class BatchedServer:
                 if len(running) >= self.max_slots or self.used_bytes + need > self.budget:
                     break
                 small = w <= self.small_work
-                if not small and running and work + w > self.work_budget:
-                    k += 1  # this one waits; later small ones may still join
+                if not small and (large_blocked or (work > 0 and work + w > self.work_budget)):
+                    # this one waits, and so does every large request behind it
+                    # (no overtaking, so the largest requests cannot starve);
+                    # later small ones may still join
+                    large_blocked = True
+                    k += 1
                     continue
                 slot = ens.add(p, v, m, self.dt, r["steps"])
                 if slot is None:  # arena full: wait for retirements
                     break
+                sub = self._sub(r["n"])
+                if sub > 1:
+                    ens.set_substeps(slot, sub)
                 del ready[k]
                 self.used_bytes += need
-                work += w
+                if not small:
+                    work += w
                 running[slot] = r
-                remaining[slot] = r["steps"] + 1
+                remaining[slot] = 1 + -(-r["steps"] // sub)  # initial forces + ticks
                 records[r["id"]] = {"n": r["n"], "steps": r["steps"], "arrival": r["arrival"],
                                     "admit": time.perf_counter() - t0}
             if not running:
                 if pending and not ready:
                     wait = pending[0]["arrival"] - (time.perf_counter() - t0)
                     if wait > 0:
-                        time.sleep(min(wait, 0.05))
+                        time.sleep(min(wait, 0.005))
                 continue
             # Run ticks until the next request finishes (known on the host),
             # bounded so arrivals are admitted within a few ticks.
@@ -168,8 +172,101 @@ class BatchedServer:
                 rec = records[r["id"]]
                 rec["finish"] = time.perf_counter() - t0
                 rec["latency"] = rec["finish"] - rec["arrival"]
-        wall = time.perf_counter() - t0
-        return records, states, {"wall_s": wall, "ticks": ticks, "host_and_gpu_tick_s": busy_s}
+        return records, states, {"ticks": ticks, "host_and_gpu_tick_s": busy_s}
+
+
+class BatchedServer:
+    """Continuous batching: a main lane (one ensemble arena) and, for small
+    requests, an express lane (a second ensemble on its own stream whose
+    persistent force launch holds a few CTA slots that the main lane leaves
+    free), so small requests run at their own tick pace beside the large
+    ones instead of in lockstep with them."""
+
+    def __init__(self, eps2: float = 1e-4, dt: float = 0.005, budget_bytes: float = 120e9,
+                 max_slots: int = 512, max_bodies: int | None = None,
+                 max_ticks_per_sync: int = 32, work_budget: float = 2e10,
+                 small_work: float = 1e8, sub_work: float = 0.0, express_n: int = 8192,
+                 express_ctas: int = 32, express_slots: int = 256):
+        """work_budget: interactions per step of the large requests running
+        above which further large requests wait (first come first served)
+        instead of joining -- about what saturates the GPU, so joining would
+        only slow everyone; small requests (N^2 <= small_work) always join
+        (slots and memory allowing) and do not count against it.
+        sub_work: a request takes sub = min(8, sub_work // N^2) (at least 1)
+        steps per tick (0: one step per tick).
+        express_n: requests with N <= express_n go to the express lane
+        (express_ctas CTA slots, express_slots systems); 0 = one lane."""
+        from . import Ensemble
+        self.dt = dt
+        self.budget = budget_bytes
+        self.max_slots = max_slots
+        self.express = None
+        self.express_n = express_n
+        ex_budget = 0.0
+        if express_n > 0:
+            ex_budget = min(budget_bytes / 4, express_slots * express_n * BYTES_PER_BODY)
+            ex = Ensemble(express_slots * express_n, express_slots, eps2)
+            ex.set_grid(express_ctas)
+            self.express = _Lane(ex, ex_budget, express_slots, dt, max_ticks_per_sync,
+                                 work_budget, small_work, sub_work)
+        main_budget = budget_bytes - ex_budget
+        if max_bodies is None:
+            max_bodies = int(min(main_budget // BYTES_PER_BODY, 32 << 20))
+        ens = Ensemble(max_bodies, max_slots, eps2)
+        if self.express is not None:
+            ens.set_grid(ens.max_grid() - express_ctas)
+        self.main = _Lane(ens, main_budget, max_slots, dt, max_ticks_per_sync, work_budget,
+                          small_work, sub_work)
+        self.ens = ens  # the main lane's ensemble
+
+    @property
+    def used_bytes(self):
+        return self.main.used_bytes + (self.express.used_bytes if self.express else 0)
+
+    def close(self):
+        self.main.ens.close()
+        if self.express is not None:
+            self.express.ens.close()
+
+    def run(self, requests, keep_states=(), time_limit: float | None = None):
+        """Serve `requests` (dicts with n, steps, seed, arrival) in real time.
+        Returns per-request records and, for ids in keep_states, final states.
+        The lanes run in two host threads (the library's calls release the
+        interpreter lock); latency = completion time - arrival time."""
+        import threading
+        if self.express is not None:
+            small = [r for r in requests if r["n"] <= self.express_n]
+            large = [r for r in requests if r["n"] > self.express_n]
+        else:
+            small, large = [], list(requests)
+        t0 = time.perf_counter()
+        out = {}
+        errors = []
+
+        def express_lane():
+            try:
+                out["express"] = self.express.serve(small, t0, keep_states, time_limit)
+            except BaseException as exc:  # re-raised in the caller's thread
+                errors.append(exc)
+
+        th = None
+        if small:
+            th = threading.Thread(target=express_lane)
+            th.start()
+        out["main"] = self.main.serve(large, t0, keep_states, time_limit)
+        if th is not None:
+            th.join()
+        if errors:
+            raise errors[0]
+        records, states, info = {}, {}, {"wall_s": time.perf_counter() - t0, "ticks": 0,
+                                         "host_and_gpu_tick_s": 0.0, "lanes": {}}
+        for name, (rec, st, inf) in out.items():
+            records.update(rec)
+            states.update(st)
+            info["ticks"] += inf["ticks"]
+            info["host_and_gpu_tick_s"] += inf["host_and_gpu_tick_s"]
+            info["lanes"][name] = dict(inf, requests=len(rec))
+        return records, states, info
 
 
 def plain_service_time(req, eps2: float, dt: float) -> float:
@@ -199,10 +296,15 @@ def _pct(x, q):
     return float(np.percentile(np.asarray(x), q)) if len(x) else None
 
 
-def _batched_run(reqs, eps2, dt, budget_gb, slots, work_budget=2e10):
-    srv = BatchedServer(eps2, dt, budget_gb * 1e9, slots, work_budget=work_budget)
+def _batched_run(reqs, eps2, dt, budget_gb, slots, work_budget=2e10, sub_work=0.0,
+                 records_out=None, express_n=8192, express_ctas=32):
+    srv = BatchedServer(eps2, dt, budget_gb * 1e9, slots, work_budget=work_budget,
+                        sub_work=sub_work, express_n=express_n, express_ctas=express_ctas)
     recs, _, info = srv.run(reqs)
     srv.close()
+    if records_out is not None:
+        records_out.append({"work_budget": work_budget, "sub_work": sub_work,
+                            "express_n": express_n, "records": recs})
     lat = [r["latency"] for r in recs.values() if "latency" in r]
     inter = sum(float(r["n"]) ** 2 * (r["steps"] + 1) for r in recs.values() if "latency" in r)
     span = max(r["finish"] for r in recs.values() if "finish" in r) - min(
@@ -212,13 +314,15 @@ def _batched_run(reqs, eps2, dt, budget_gb, slots, work_budget=2e10):
             "interactions_per_s": inter / span, "latency_p50_s": _pct(lat, 50),
             "latency_p99_s": _pct(lat, 99),
             "latency_mean_s": float(np.mean(lat)) if lat else None,
-            "work_budget": work_budget}
+            "work_budget": work_budget, "sub_work": sub_work, "express_n": express_n,
+            "express_ctas": express_ctas, "lanes": info.get("lanes")}
 
 
 def serve_study(n_req: int = 20000, rates=(10.0,), seed: int = 5, n_lo: int = 256,
                 n_hi: int = 65536, steps_lo: int = 10, steps_hi: int = 1000, dt: float = 0.005,
                 eps2: float = 1e-4, budget_gb: float = 120.0, slots: int = 512,
-                plain_sample: int | None = None, work_budgets=(2e10,)) -> dict:
+                plain_sample: int | None = None, work_budgets=(2e10,), sub_work: float = 0.0,
+                records_out=None, express_n: int = 8192, express_ctas: int = 32) -> dict:
     """Both servers on the same stream at each arrival rate.  The plain
     server's per-request service times are measured once (they do not depend
     on the arrival times) and replayed through the FIFO rule at every rate.
@@ -249,7 +353,8 @@ def serve_study(n_req: int = 20000, rates=(10.0,), seed: int = 5, n_lo: int = 25
            "plain_service_predicted": len(measured) != n_req, "by_rate": []}
     for rate in rates:
         reqs = make_requests(n_req, rate, seed, n_lo, n_hi, steps_lo, steps_hi)
-        runs = [_batched_run(reqs, eps2, dt, budget_gb, slots, wb) for wb in work_budgets]
+        runs = [_batched_run(reqs, eps2, dt, budget_gb, slots, wb, sub_work, records_out,
+                             express_n, express_ctas) for wb in work_budgets]
         b = runs[0]
         arrivals = [r["arrival"] for r in reqs]
         pfin = fifo_finish_times(arrivals, service)
@@ -284,11 +389,24 @@ def main(argv=None):
                     help="comma-separated interactions per tick above which large requests "
                          "wait; the batched server runs once per value, the first is the "
                          "headline")
+    ap.add_argument("--sub-work", type=float, default=0.0,
+                    help="a request takes min(8, sub_work // N^2) steps per tick (0: one)")
+    ap.add_argument("--express-n", type=int, default=8192,
+                    help="requests with N <= this run in the express lane (0: one lane)")
+    ap.add_argument("--express-ctas", type=int, default=32,
+                    help="CTA slots of the express lane's persistent force launch")
+    ap.add_argument("--records", default=None,
+                    help="write every batched request's record (JSON) to this path")
     a = ap.parse_args(argv)
     rates = [float(x) for x in a.rates.split(",")]
     budgets = [float(x) for x in a.work_budgets.split(",")]
+    recs = [] if a.records else None
     r = serve_study(a.requests, rates, a.seed, a.n_lo, a.n_hi, a.steps_lo, a.steps_hi, a.dt,
-                    a.eps2, a.budget_gb, a.slots, a.plain_sample, budgets)
+                    a.eps2, a.budget_gb, a.slots, a.plain_sample, budgets, a.sub_work, recs,
+                    a.express_n, a.express_ctas)
+    if a.records:
+        with open(a.records, "w") as f:
+            json.dump(recs, f)
     print(json.dumps(r))
 
 

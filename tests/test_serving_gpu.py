@@ -35,7 +35,8 @@ def test_results_identical_alone_and_in_the_mix(cuda):
 def test_tiny_budget_admits_within_limits(cuda):
     reqs = _stream(10, float("inf"), 4)
     biggest = max(r["n"] for r in reqs) * serving.BYTES_PER_BODY
-    srv = serving.BatchedServer(1e-4, 0.005, budget_bytes=1.5 * biggest, max_slots=3)
+    srv = serving.BatchedServer(1e-4, 0.005, budget_bytes=1.5 * biggest, max_slots=3,
+                                express_n=0)  # one lane: every request in the main arena
     peak = {"bytes": 0, "slots": 0}
     orig_add = srv.ens.add
 
@@ -66,3 +67,27 @@ def test_matches_plain_single_system(cuda):
     pe, ve, _ = st[r["id"]]
     assert np.abs(pe - ps).max() <= 1e-8 * np.abs(ps).max()
     assert np.abs(ve - vs).max() <= 1e-7 * np.abs(vs).max()
+
+
+def test_express_lane_admits_within_its_limits(cuda):
+    """Small requests run in the express lane, within its slot count and its
+    share of the state budget; its arena runs beside the main one."""
+    reqs = _stream(10, float("inf"), 4)  # N <= 6000: all express
+    srv = serving.BatchedServer(1e-4, 0.005, 4e9, 8, express_slots=3)
+    lane = srv.express
+    assert srv.ens.max_grid() == lane.ens.max_grid()
+    peak = {"bytes": 0, "slots": 0}
+    orig_add = lane.ens.add
+
+    def add(*a, **k):
+        slot = orig_add(*a, **k)
+        peak["bytes"] = max(peak["bytes"], lane.used_bytes + a[0].shape[0] * serving.BYTES_PER_BODY)
+        peak["slots"] = max(peak["slots"], lane.ens.active())
+        return slot
+
+    lane.ens.add = add
+    recs, _, info = srv.run(reqs)
+    srv.close()
+    assert all("latency" in r for r in recs.values())
+    assert info["lanes"]["express"]["requests"] == 10 and info["lanes"]["main"]["requests"] == 0
+    assert 0 < peak["slots"] <= 3 and peak["bytes"] <= lane.budget
