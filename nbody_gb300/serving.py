@@ -186,7 +186,7 @@ class BatchedServer:
                  max_slots: int = 512, max_bodies: int | None = None,
                  max_ticks_per_sync: int = 32, work_budget: float = 2e10,
                  small_work: float = 1e8, sub_work: float = 0.0, express_n: int = 8192,
-                 express_ctas: int = 32, express_slots: int = 256):
+                 express_ctas: int = 32, express_slots: int = 256, ensemble_factory=None):
         """work_budget: interactions per step of the large requests running
         above which further large requests wait (first come first served)
         instead of joining -- about what saturates the GPU, so joining would
@@ -195,8 +195,11 @@ class BatchedServer:
         sub_work: a request takes sub = min(8, sub_work // N^2) (at least 1)
         steps per tick (0: one step per tick).
         express_n: requests with N <= express_n go to the express lane
-        (express_ctas CTA slots, express_slots systems); 0 = one lane."""
-        from . import Ensemble
+        (express_ctas CTA slots, express_slots systems); 0 = one lane.
+        ensemble_factory(max_bodies, max_systems, eps2): the arena type
+        (default nbody_gb300.Ensemble; tests pass a host-side stand-in)."""
+        if ensemble_factory is None:
+            from . import Ensemble as ensemble_factory
         self.dt = dt
         self.budget = budget_bytes
         self.max_slots = max_slots
@@ -205,14 +208,14 @@ class BatchedServer:
         ex_budget = 0.0
         if express_n > 0:
             ex_budget = min(budget_bytes / 4, express_slots * express_n * BYTES_PER_BODY)
-            ex = Ensemble(express_slots * express_n, express_slots, eps2)
+            ex = ensemble_factory(express_slots * express_n, express_slots, eps2)
             ex.set_grid(express_ctas)
             self.express = _Lane(ex, ex_budget, express_slots, dt, max_ticks_per_sync,
                                  work_budget, small_work, sub_work)
         main_budget = budget_bytes - ex_budget
         if max_bodies is None:
             max_bodies = int(min(main_budget // BYTES_PER_BODY, 32 << 20))
-        ens = Ensemble(max_bodies, max_slots, eps2)
+        ens = ensemble_factory(max_bodies, max_slots, eps2)
         if self.express is not None:
             ens.set_grid(ens.max_grid() - express_ctas)
         self.main = _Lane(ens, main_budget, max_slots, dt, max_ticks_per_sync, work_budget,
