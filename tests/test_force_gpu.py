@@ -12,7 +12,7 @@ import nbody_gb300 as nb
 
 pytestmark = pytest.mark.gpu
 
-# Per-body |F - F_ref| / |F_ref| against the reference's CPU_AOS (north-star
+# Per-body |F - F_ref| / |F_ref| against the reference's CPU_AOS (the path's
 # accuracy gate), and against the FP64 all-pairs sum of the same FP32 inputs.
 # On the golden fixtures the reference's own CPU_AOS is up to 1.8e-6 (RMS
 # 1.7e-7) from FP64 and a sequential IEEE binary32 sum up to 3.1e-6 (RMS

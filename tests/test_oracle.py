@@ -7,7 +7,7 @@ from conftest import GOLDEN_FORCE_CASES, golden
 from oracle import oracle as O
 
 # Per-body norm-wise tolerance of an FP32 all-pairs force against the
-# reference's CPU_AOS (spec accuracy gate).
+# reference's CPU_AOS (the per-body accuracy gate of the force path).
 FORCE_TOL = 1e-5
 
 
