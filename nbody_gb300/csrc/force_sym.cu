@@ -3,17 +3,19 @@
 // unregistered tiled kernels, src/nbody_GPU_AOS_tiled.cu:93-179, which add
 // every pair's contribution with per-pair warp reductions and float atomics).
 //
-// Here the unit of work is a block pair (bi, bj), bi <= bj, of 1024-body
-// blocks, one CTA of 8 warps each:
-//   * warp w holds 128 targets of block bi in registers (4 per lane, negated
+// Here the unit of work is a block pair (bi, bj), bi <= bj, of 2048-body
+// blocks, one CTA of 8 warps each (one CTA per SM: up to 255 registers a
+// thread, spent on independent work per warp rather than on more warps):
+//   * warp w holds 256 targets of block bi in registers (8 per lane, negated
 //     and duplicated into f32x2 pairs, with their masses);
-//   * block bj is visited as 8 source sets of 128 bodies; every lane loads 4
-//     sources (2 f32x2 pairs of the j-stream) plus zeroed accumulators, and
-//     for 32 steps evaluates its 4 targets against the 4 sources it holds,
+//   * block bj is visited as 8 source sets of 256 bodies; every lane loads 8
+//     sources (4 f32x2 pairs of the j-stream) plus zeroed accumulators, and
+//     for 32 steps evaluates its 8 targets against the 8 sources it holds,
 //     then passes sources and their accumulators to the next lane
 //     (__shfl_sync rotation).  After 32 steps each source has met every
 //     target of the warp and is back in its lane with its accumulated
-//     reaction;
+//     reaction.  Each step carries 32 independent pair evaluations per lane
+//     for 28 shuffles of 64-bit values;
 //   * per pair and target: d = p_j - p_i, s = (|d|^2 + eps2)^-3/2 (MUFU
 //     rsqrt), a_i += m_j s d, a_j -= m_i s d: 16 f32x2 operations per 4
 //     interactions instead of 24 for the one-sided kernel;
@@ -26,7 +28,7 @@
 //     evaluates s == w one-sided (every ordered pair of the set once, the
 //     self pair contributing 0).
 // A final kernel rounds the FP64 accumulators to FP32 forces.  The FP64 sums
-// receive ~2 N / 1024 contributions per body in an order set by scheduling;
+// receive ~2 N / 2048 contributions per body in an order set by scheduling;
 // FP64 keeps the result order-independent to well below FP32 resolution.
 #include <cuda_runtime.h>
 
@@ -41,11 +43,15 @@ namespace sym {
 
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
-constexpr int KI = 4;                        // targets per lane
-constexpr int KJ = 4;                        // sources per lane (2 f32x2 pairs)
+constexpr int KI = 8;                        // targets per lane
+constexpr int KJ = 8;                        // sources per lane (4 f32x2 pairs)
+constexpr int NC = KJ / 2;                   // f32x2 source pairs per lane
+constexpr int kMinBlocks = 1;                // resident CTAs per SM (register cap)
 constexpr int kSet = 32 * KJ;                // sources per set
 constexpr int kBlock = kWarps * 32 * KI;     // bodies per block (1024)
 static_assert(kBlock == kWarps * kSet, "a block is 8 source sets");
+constexpr int kFoldSets = kSet >= 256 ? 1 : 256 / kSet;  // sets per compensated fold
+static_assert(kWarps % kFoldSets == 0, "folds end with the block's last set");
 
 struct Params {
     const float4 *__restrict__ pm;  // AOS posMass (targets), n bodies
@@ -78,8 +84,9 @@ __device__ __forceinline__ void pair_of(long long p, int nb, int &bi, int &bj) {
 // sources' reactions (both sides); otherwise only the targets' sums.  The
 // branch on REACT is resolved at compile time, outside the step loop.
 template <bool REACT>
-__device__ __forceinline__ void rotate_set(f2 (&sx)[2], f2 (&sy)[2], f2 (&sz)[2], f2 (&sm)[2],
-                                           f2 (&rx)[2], f2 (&ry)[2], f2 (&rz)[2],
+__device__ __forceinline__ void rotate_set(f2 (&sx)[NC], f2 (&sy)[NC], f2 (&sz)[NC],
+                                           f2 (&sm)[NC], f2 (&rx)[NC], f2 (&ry)[NC],
+                                           f2 (&rz)[NC],
                                            const f2 (&nx)[KI], const f2 (&ny)[KI],
                                            const f2 (&nz)[KI], const f2 (&nm)[KI], f2 (&ax)[KI],
                                            f2 (&ay)[KI], f2 (&az)[KI], f2 eps2p, int lane) {
@@ -87,7 +94,7 @@ __device__ __forceinline__ void rotate_set(f2 (&sx)[2], f2 (&sy)[2], f2 (&sz)[2]
 #pragma unroll 2
     for (int step = 0; step < 32; step++) {
 #pragma unroll
-        for (int c = 0; c < 2; c++) {
+        for (int c = 0; c < NC; c++) {
 #pragma unroll
             for (int k = 0; k < KI; k++) {
                 f2 dx = f2_add(sx[c], nx[k]);
@@ -115,7 +122,7 @@ __device__ __forceinline__ void rotate_set(f2 (&sx)[2], f2 (&sy)[2], f2 (&sz)[2]
         }
         // pass sources (and their reactions) to the next lane
 #pragma unroll
-        for (int c = 0; c < 2; c++) {
+        for (int c = 0; c < NC; c++) {
             sx[c] = __shfl_sync(0xffffffffu, sx[c], from);
             sy[c] = __shfl_sync(0xffffffffu, sy[c], from);
             sz[c] = __shfl_sync(0xffffffffu, sz[c], from);
@@ -129,7 +136,7 @@ __device__ __forceinline__ void rotate_set(f2 (&sx)[2], f2 (&sy)[2], f2 (&sz)[2]
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 2) sym_kernel(Params P) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) sym_kernel(Params P) {
     __shared__ float red[kWarps][3][kSet];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     int bi, bj;
@@ -159,11 +166,11 @@ __global__ void __launch_bounds__(kThreads, 2) sym_kernel(Params P) {
     for (int s = 0; s < kWarps; s++) {
         // mode: 2 both sides, 1 targets only (the warp's own set), 0 skip
         const int mode = !diag ? 2 : (s > warp ? 2 : (s == warp ? 1 : 0));
-        // sources of set s: lane holds bodies base + lane*4 .. +3 (2 pairs)
+        // sources of set s: lane holds bodies base .. base + KJ - 1 (NC pairs)
         const int base = bj * kBlock + s * kSet + lane * KJ;
-        f2 sx[2], sy[2], sz[2], sm[2], rx[2], ry[2], rz[2];
+        f2 sx[NC], sy[NC], sz[NC], sm[NC], rx[NC], ry[NC], rz[NC];
 #pragma unroll
-        for (int c = 0; c < 2; c++) {
+        for (int c = 0; c < NC; c++) {
             const ulonglong2 a = reinterpret_cast<const ulonglong2 *>(P.js)[base + 2 * c];
             const ulonglong2 b = reinterpret_cast<const ulonglong2 *>(P.js)[base + 2 * c + 1];
             sx[c] = a.x;
@@ -176,8 +183,8 @@ __global__ void __launch_bounds__(kThreads, 2) sym_kernel(Params P) {
             rotate_set<true>(sx, sy, sz, sm, rx, ry, rz, nx, ny, nz, nm, ax, ay, az, eps2p, lane);
         else if (mode == 1)
             rotate_set<false>(sx, sy, sz, sm, rx, ry, rz, nx, ny, nz, nm, ax, ay, az, eps2p, lane);
-        // fold target sums into the compensated sums every 2 sets (256 sources)
-        if (s & 1) {
+        // fold target sums into the compensated sums every 256 sources
+        if ((s + 1) % kFoldSets == 0) {
 #pragma unroll
             for (int k = 0; k < KI; k++) {
                 float l, h;
@@ -192,7 +199,7 @@ __global__ void __launch_bounds__(kThreads, 2) sym_kernel(Params P) {
         }
         // reactions on set s: stage per warp, add in warp order, FP64 atomics
 #pragma unroll
-        for (int c = 0; c < 2; c++) {
+        for (int c = 0; c < NC; c++) {
             float l, h;
             f2_unpack(rx[c], l, h);
             red[warp][0][lane * KJ + 2 * c] = l;
