@@ -247,6 +247,16 @@ NBGB_API int nbgb_ensemble_set_substeps(nbgb_ensemble *ens, int slot, int sub);
    together fit the resident slots run side by side on their own streams. */
 NBGB_API int nbgb_ensemble_set_grid(nbgb_ensemble *ens, int ctas);
 NBGB_API int nbgb_ensemble_max_grid(nbgb_ensemble *ens);
+/* Systems admitted afterwards with N >= nmin are evaluated with the
+   Newton's-third-law kernel (as nbgb_force_newton3: each pair once, FP64
+   block-pair sums) instead of the work queue; 0 = none (the default).  Their
+   results repeat to FP64 rounding order rather than bit for bit.  The first
+   nonzero call allocates an FP64 sums arena (24 B per body of capacity). */
+NBGB_API int nbgb_ensemble_set_newton3_min(nbgb_ensemble *ens, size_t nmin);
+/* high != 0: the ensemble's stream gets the device's greatest priority, so
+   its CTAs are dispatched ahead of other streams' pending ones (an ensemble
+   running beside a busier one).  Drains and recreates the stream. */
+NBGB_API int nbgb_ensemble_set_priority(nbgb_ensemble *ens, int high);
 NBGB_API int nbgb_ensemble_remove(nbgb_ensemble *ens, int slot);
 NBGB_API int nbgb_ensemble_active(nbgb_ensemble *ens);
 NBGB_API void *nbgb_ensemble_stream(nbgb_ensemble *ens);

@@ -377,6 +377,15 @@ class Ensemble:
     def max_grid(self) -> int:
         return int(self.lib.nbgb_ensemble_max_grid(self.h))
 
+    def set_priority(self, high: bool):
+        """High: the ensemble's stream gets the device's greatest priority."""
+        check(self.lib.nbgb_ensemble_set_priority(self.h, int(high)), "ensemble_set_priority")
+
+    def set_newton3_min(self, nmin: int):
+        """Systems admitted afterwards with N >= nmin use the Newton's-third-
+        law kernel (0 = none); results then repeat to FP64 rounding order."""
+        check(self.lib.nbgb_ensemble_set_newton3_min(self.h, nmin), "ensemble_set_newton3_min")
+
     def remove(self, slot: int):
         check(self.lib.nbgb_ensemble_remove(self.h, slot), "ensemble_remove")
         self._n.pop(slot, None)

@@ -78,6 +78,8 @@ SIGNATURES = {
     "nbgb_ensemble_set_substeps": (ctypes.c_int, [c_vp, ctypes.c_int, ctypes.c_int]),
     "nbgb_ensemble_set_grid": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "nbgb_ensemble_max_grid": (ctypes.c_int, [c_vp]),
+    "nbgb_ensemble_set_newton3_min": (ctypes.c_int, [c_vp, ctypes.c_size_t]),
+    "nbgb_ensemble_set_priority": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "nbgb_ensemble_active": (ctypes.c_int, [c_vp]),
     "nbgb_ensemble_stream": (c_vp, [c_vp]),
     "nbgb_ic_reference": (ctypes.c_int, [c_f32p, c_f32p, c_size, ctypes.c_float,

@@ -20,6 +20,12 @@
 //                    (last item of the i-block, atomic counter)
 //   ens_kick         v += a dt/2 for moving systems
 //
+// Newton-3 systems (opt-in, nbgb_ensemble_set_newton3_min): systems of at
+// least that many bodies skip the work queue; pass 0 of each tick evaluates
+// them with the Newton's-third-law kernel (block pairs, FP64 sums; one launch
+// for all of them) and rounds their sums to FP32 accelerations.  Their
+// results repeat to FP64 rounding order (not bit for bit).
+//
 // Sub-cycling: a system may take up to kMaxSub steps per tick (its `sub`).
 // A tick then runs passes p = 0 .. max sub - 1, each the three launches above
 // over the systems whose effective sub (min(sub, steps left)) exceeds p, so
@@ -487,12 +493,14 @@ struct HostSys {
     long long steps_done = 0;
     bool log_mass = false;  // every mass >= 0: log-domain pairs (kLogMass)
     int sub = 1;            // steps per tick (1..kMaxSub)
+    bool n3 = false;        // Newton-3 system (no work items)
+    size_t acc_off = 0, acc_len = 0;  // its FP64 sums ([3][npad] doubles)
 };
 
 // Steps a system takes in the coming tick (0 before its initial forces).
 inline int sub_eff(const HostSys &h) {
-    if (!h.started)
-        return 1;  // the initial-force pass
+    if (!h.started || h.n3)
+        return 1;  // the initial-force pass; Newton-3 systems run in pass 0 only
     return (int)std::min<long long>(h.sub, h.steps_left);
 }
 
@@ -528,6 +536,13 @@ struct nbgb_ensemble {
     BucketPlan bucket[32];
     int n_items = 0, n_slots = 0;
     int n_pass = 1;                       // passes per tick (max effective sub)
+    // Newton-3 systems
+    size_t n3_min = 0;                    // 0: off
+    double *acc64 = nullptr;              // FP64 sums arena (allocated when enabled)
+    size_t acc64_cap = 0;
+    RangeAlloc a_acc;
+    nbgb::SymSystem *d_sym = nullptr, *h_sym = nullptr;
+    int n_sym = 0;
     int pass_first[nbgb::ens::kMaxSub];   // first item of pass p (items sorted by sub)
     bool dirty = true;
     cudaGraphExec_t graph = nullptr;
@@ -611,6 +626,8 @@ int rebuild(nbgb_ensemble *e) {
             e->h_desc[s].flags = 0;
             continue;
         }
+        if (h.n3)
+            continue;  // evaluated by the Newton-3 launch
         const int bi = nbgb::ens::kThreads * ((h.variant == 0 || h.variant == 2) ? 1 : 2);
         for (int b = 0; b < h.nblocks; b++)
             for (int r = 0; r < h.nsplit; r++) {
@@ -654,7 +671,30 @@ int rebuild(nbgb_ensemble *e) {
             e->h_slot_sys[q] = s;
     }
     e->n_slots = n_pairs;
+    // Newton-3 systems of this tick, with their block-pair prefix counts
+    e->n_sym = 0;
+    long long pairs = 0;
+    const int sb = nbgb::sym_block_bodies();
+    for (int s = 0; s < e->max_systems; s++) {
+        const HostSys &h = e->sys[s];
+        if (!h.used || !h.n3 || !(h.steps_left > 0 || !h.started))
+            continue;
+        nbgb::SymSystem &t = e->h_sym[e->n_sym++];
+        t.pm = e->pm + h.body_off;
+        t.js = e->js + h.js_off;
+        t.acc = e->acc64 + h.acc_off;
+        t.out = e->acc + h.body_off;
+        t.n = h.n;
+        t.npad = (int)(h.js_len);
+        t.nblocks = (int)(h.js_len / sb);
+        t.eps2 = e->eps2;
+        t.pair_begin = pairs;
+        pairs += (long long)t.nblocks * (t.nblocks + 1) / 2;
+    }
     cudaStream_t st = e->stream;
+    if (e->n_sym && cudaMemcpyAsync(e->d_sym, e->h_sym, sizeof(nbgb::SymSystem) * e->n_sym,
+                                    cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return NBGB_ERR_CUDA;
     if (cudaMemcpyAsync(e->d_desc, e->h_desc, sizeof(Desc) * e->max_systems,
                         cudaMemcpyHostToDevice, st) != cudaSuccess ||
         (e->n_items &&
@@ -698,6 +738,11 @@ int launch_tick(nbgb_ensemble *e) {
         if (n_items > 0)
             nbgb::ens::ens_force_kernel<<<e->grid, nbgb::ens::kThreads,
                                           nbgb::ens::kStages * nbgb::ens::kStageBytes, st>>>(P);
+        if (pass == 0 && e->n_sym > 0) {
+            const int rc = nbgb::launch_sym_systems(e->d_sym, e->h_sym, e->n_sym, st);
+            if (rc != NBGB_OK)
+                return rc;
+        }
         nbgb::ens::ens_kdk_kernel<<<nb, tb, 0, st>>>(e->d_desc, e->d_slot_sys, e->n_slots,
                                                      e->x64, e->max_bodies, e->mass, e->acc,
                                                      e->pm, e->js, 1, pass);
@@ -719,6 +764,9 @@ void free_ens(nbgb_ensemble *e) {
     cudaFree(e->d_desc);
     cudaFree(e->d_items);
     cudaFree(e->d_slot_sys);
+    cudaFree(e->acc64);
+    cudaFree(e->d_sym);
+    cudaFreeHost(e->h_sym);
     cudaFreeHost(e->h_desc);
     cudaFreeHost(e->h_items);
     cudaFreeHost(e->h_slot_sys);
@@ -743,8 +791,10 @@ NBGB_API nbgb_ensemble *nbgb_ensemble_create(size_t max_bodies, int max_systems,
     e->eps2 = softeningSquared;
     e->max_systems = max_systems;
     e->max_bodies = max_bodies;
-    // j-stream: bodies rounded up to tiles (<= 1024 per system) and to pairs
-    e->js_cap = max_bodies + (size_t)max_systems * nbgb::ens::kMaxJT;
+    // j-stream: bodies rounded up to tiles (<= 1024 per system) or to
+    // Newton-3 blocks, and to pairs
+    e->js_cap = max_bodies +
+                (size_t)max_systems * std::max(nbgb::ens::kMaxJT, nbgb::sym_block_bodies());
     e->js_cap += e->js_cap & 1;
     // split partials: hi + lo for up to 4-way j-splits of every body (plus
     // block padding); counters and items for up to 4 splits of 256-body blocks
@@ -772,6 +822,8 @@ NBGB_API nbgb_ensemble *nbgb_ensemble_create(size_t max_bodies, int max_systems,
     ok = ok && cudaMallocHost(&e->h_desc, sizeof(Desc) * max_systems) == cudaSuccess;
     ok = ok && cudaMallocHost(&e->h_items, sizeof(int4) * e->items_cap) == cudaSuccess;
     ok = ok && cudaMallocHost(&e->h_slot_sys, sizeof(int) * (e->js_cap / 2)) == cudaSuccess;
+    ok = ok && cudaMalloc(&e->d_sym, sizeof(nbgb::SymSystem) * max_systems) == cudaSuccess;
+    ok = ok && cudaMallocHost(&e->h_sym, sizeof(nbgb::SymSystem) * max_systems) == cudaSuccess;
     ok = ok && cudaMemsetAsync(e->cnt, 0, e->cnt_cap * 4, e->stream) == cudaSuccess;
     ok = ok && cudaMemsetAsync(e->js, 0, e->js_cap * 16, e->stream) == cudaSuccess;
     ok = ok && cudaFuncSetAttribute(nbgb::ens::ens_force_kernel,
@@ -843,15 +895,30 @@ NBGB_API int nbgb_ensemble_add(nbgb_ensemble *e, const double *pos3, const doubl
     h.n = (int)n;
     choose_plan(e, (int)n, h);
     h.body_len = n;
-    h.js_len = (size_t)h.ntiles * h.jt;
-    h.js_len += h.js_len & 1;
-    h.part_len = h.nsplit > 1 ? 2 * (size_t)h.nsplit * h.ni_pad : 0;
-    h.cnt_len = h.nsplit > 1 ? (size_t)h.nblocks : 0;
-    size_t ob, oj, op = 0, oc = 0;
-    if (!e->a_body.alloc(h.body_len, 1, ob))
+    h.n3 = e->n3_min > 0 && n >= e->n3_min;
+    if (h.n3) {  // j-stream padded to whole Newton-3 blocks, FP64 sums
+        const size_t sb = (size_t)nbgb::sym_block_bodies();
+        h.js_len = (n + sb - 1) / sb * sb;
+        h.acc_len = 3 * h.js_len;
+        h.part_len = h.cnt_len = 0;
+    } else {
+        h.js_len = (size_t)h.ntiles * h.jt;
+        h.js_len += h.js_len & 1;
+        h.part_len = h.nsplit > 1 ? 2 * (size_t)h.nsplit * h.ni_pad : 0;
+        h.cnt_len = h.nsplit > 1 ? (size_t)h.nblocks : 0;
+    }
+    size_t ob, oj, op = 0, oc = 0, oa = 0;
+    if (h.acc_len && !e->a_acc.alloc(h.acc_len, 32, oa))
         return NBGB_ERR_NO_MEMORY;
+    if (!e->a_body.alloc(h.body_len, 1, ob)) {
+        if (h.acc_len)
+            e->a_acc.release(oa, h.acc_len);
+        return NBGB_ERR_NO_MEMORY;
+    }
     if (!e->a_js.alloc(h.js_len, 2, oj)) {
         e->a_body.release(ob, h.body_len);
+        if (h.acc_len)
+            e->a_acc.release(oa, h.acc_len);
         return NBGB_ERR_NO_MEMORY;
     }
     if (h.part_len && !e->a_part.alloc(h.part_len, 2, op)) {
@@ -866,6 +933,7 @@ NBGB_API int nbgb_ensemble_add(nbgb_ensemble *e, const double *pos3, const doubl
             e->a_part.release(op, h.part_len);
         return NBGB_ERR_NO_MEMORY;
     }
+    h.acc_off = oa;
     h.body_off = ob;
     h.js_off = oj;
     h.part_off = op;
@@ -873,7 +941,7 @@ NBGB_API int nbgb_ensemble_add(nbgb_ensemble *e, const double *pos3, const doubl
     h.dt = dt;
     h.steps_left = steps;
     h.used = true;
-    h.log_mass = true;
+    h.log_mass = !h.n3;  // the Newton-3 kernel reads plain masses
     for (size_t i = 0; i < n && h.log_mass; i++)
         h.log_mass = mass[i] >= 0.f;
     // upload state (SoA FP64, masses), zero the j-stream range
@@ -891,6 +959,8 @@ NBGB_API int nbgb_ensemble_add(nbgb_ensemble *e, const double *pos3, const doubl
     if (cudaMemcpyAsync(e->mass + ob, mass, n * sizeof(float), cudaMemcpyHostToDevice, st) !=
             cudaSuccess ||
         cudaMemsetAsync(e->js + oj, 0, h.js_len * 16, st) != cudaSuccess ||
+        (h.acc_len &&
+         cudaMemsetAsync(e->acc64 + oa, 0, h.acc_len * sizeof(double), st) != cudaSuccess) ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return NBGB_ERR_CUDA;
     e->sys[s] = h;
@@ -1062,6 +1132,50 @@ NBGB_API int nbgb_ensemble_set_substeps(nbgb_ensemble *e, int slot, int sub) {
     return NBGB_OK;
 }
 
+// Stream priority of the ensemble's work: high = the device's greatest
+// priority, so that its CTAs are dispatched ahead of other streams' pending
+// CTAs as SMs free up (an ensemble beside a busier one).  Recreates the
+// stream (after draining it).
+NBGB_API int nbgb_ensemble_set_priority(nbgb_ensemble *e, int high) {
+    if (!e)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    int lo = 0, hi = 0;
+    if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
+        cudaStreamSynchronize(e->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, high ? hi : lo) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    if (e->graph) {
+        cudaGraphExecDestroy(e->graph);
+        e->graph = nullptr;
+    }
+    cudaStreamDestroy(e->stream);
+    e->stream = st;
+    return NBGB_OK;
+}
+
+// Systems admitted from now on with at least nmin bodies use the Newton-3
+// kernel (0: none).  The first nonzero call allocates the FP64 sums arena
+// (24 B per body of capacity).
+NBGB_API int nbgb_ensemble_set_newton3_min(nbgb_ensemble *e, size_t nmin) {
+    if (!e)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (nmin > 0 && !e->acc64) {
+        const size_t cap = 3 * (e->max_bodies + (size_t)e->max_systems *
+                                                    (size_t)nbgb::sym_block_bodies());
+        if (cudaMalloc(&e->acc64, cap * sizeof(double)) != cudaSuccess) {
+            e->acc64 = nullptr;
+            return NBGB_ERR_NO_MEMORY;
+        }
+        e->acc64_cap = cap;
+        e->a_acc.init(cap);
+        e->bytes_total += cap * sizeof(double);
+    }
+    e->n3_min = nmin;
+    return NBGB_OK;
+}
+
 // Retire a slot: its arena ranges and slot become free for admission.
 NBGB_API int nbgb_ensemble_remove(nbgb_ensemble *e, int slot) {
     if (!e || slot < 0 || slot >= e->max_systems || !e->sys[slot].used)
@@ -1076,6 +1190,8 @@ NBGB_API int nbgb_ensemble_remove(nbgb_ensemble *e, int slot) {
         e->a_part.release(h.part_off, h.part_len);
     if (h.cnt_len)
         e->a_cnt.release(h.cnt_off, h.cnt_len);
+    if (h.acc_len)
+        e->a_acc.release(h.acc_off, h.acc_len);
     h = HostSys();
     e->dirty = true;
     return NBGB_OK;

@@ -136,14 +136,13 @@ __device__ __forceinline__ void rotate_set(f2 (&sx)[NC], f2 (&sy)[NC], f2 (&sz)[
     }
 }
 
-__global__ void __launch_bounds__(kThreads, kMinBlocks) sym_kernel(Params P) {
+// One block pair (bi, bj) of one system, by the whole CTA.
+__device__ __forceinline__ void sym_block_pair(const Params &P, int bi, int bj) {
     __shared__ float red[kWarps][3][kSet];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    int bi, bj;
-    pair_of(blockIdx.x, P.nblocks, bi, bj);
     const bool diag = (bi == bj);
 
-    // targets: lane owns bodies bi*1024 + warp*128 + lane + 32*k
+    // targets: lane owns bodies bi*kBlock + warp*32*KI + lane + 32*k
     f2 nx[KI], ny[KI], nz[KI], nm[KI];
     f2 ax[KI], ay[KI], az[KI];
     float hx[KI], hy[KI], hz[KI], lx[KI], ly[KI], lz[KI];
@@ -236,6 +235,52 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sym_kernel(Params P) {
     }
 }
 
+__global__ void __launch_bounds__(kThreads, kMinBlocks) sym_kernel(Params P) {
+    int bi, bj;
+    pair_of(blockIdx.x, P.nblocks, bi, bj);
+    sym_block_pair(P, bi, bj);
+}
+
+// Many systems in one launch (the ensemble's Newton-3 systems): CTA b takes
+// block pair b - pair_begin[s] of the system s whose range holds b (binary
+// search over the systems' prefix counts).
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    sym_systems_kernel(const SymSystem *__restrict__ tab, int nsys) {
+    const long long b = blockIdx.x;
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tab[mid].pair_begin <= b)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const SymSystem &t = tab[lo];
+    Params P;
+    P.pm = t.pm;
+    P.js = t.js;
+    P.acc = t.acc;
+    P.n = t.n;
+    P.npad = t.npad;
+    P.nblocks = t.nblocks;
+    P.eps2 = t.eps2;
+    int bi, bj;
+    pair_of(b - t.pair_begin, t.nblocks, bi, bj);
+    sym_block_pair(P, bi, bj);
+}
+
+// FP64 sums -> FP32 accelerations {ax, ay, az, 0}, and the sums zeroed for
+// the next evaluation.
+__global__ void sym_finish_zero_kernel(double *__restrict__ acc, int n, int npad,
+                                       float4 *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        out[i] = make_float4((float)acc[i], (float)acc[(size_t)npad + i],
+                             (float)acc[2 * (size_t)npad + i], 0.f);
+        acc[i] = acc[(size_t)npad + i] = acc[2 * (size_t)npad + i] = 0.0;
+    }
+}
+
 __global__ void sym_finish_kernel(const double *__restrict__ acc, int n, int npad,
                                   float4 *__restrict__ force) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -245,6 +290,24 @@ __global__ void sym_finish_kernel(const double *__restrict__ acc, int n, int npa
 }
 
 }  // namespace sym
+
+int launch_sym_systems(const SymSystem *d_tab, const SymSystem *h_tab, int nsys,
+                       cudaStream_t st) {
+    if (nsys <= 0)
+        return NBGB_OK;
+    const long long pairs = h_tab[nsys - 1].pair_begin +
+                            (long long)h_tab[nsys - 1].nblocks * (h_tab[nsys - 1].nblocks + 1) / 2;
+    if (pairs > (1ll << 31) - 1)
+        return NBGB_ERR_TOO_LARGE;
+    sym::sym_systems_kernel<<<(unsigned)pairs, sym::kThreads, 0, st>>>(d_tab, nsys);
+    for (int s = 0; s < nsys; s++)
+        sym::sym_finish_zero_kernel<<<(unsigned)((h_tab[s].n + 255) / 256), 256, 0, st>>>(
+            h_tab[s].acc, h_tab[s].n, h_tab[s].npad, h_tab[s].out);
+    return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
+}
+
+int sym_block_bodies() { return sym::kBlock; }
+
 }  // namespace nbgb
 
 namespace {

@@ -51,6 +51,24 @@ size_t diag_scratch_bytes();
 int launch_diagnostics(int n, const double *x64, const float *mass, const float4 *pm,
                        const float4 *vel, const float4 *phi, double *scratch, double *out8,
                        cudaStream_t st);
+// Newton-3 evaluation of many systems in one launch (the ensemble): one
+// entry per system, ordered, pair_begin = block pairs of the entries before.
+// js: paired j-stream padded with zero masses to nblocks * sym_block_bodies()
+// bodies (no log2 masses); acc: [3][npad] FP64 sums, zero on entry, left
+// zero on exit; out: FP32 accelerations.
+struct SymSystem {
+    const float4 *pm;
+    const float4 *js;
+    double *acc;
+    float4 *out;
+    int n, npad, nblocks;
+    float eps2;
+    long long pair_begin;
+};
+int launch_sym_systems(const SymSystem *d_tab, const SymSystem *h_tab, int nsys,
+                       cudaStream_t st);
+int sym_block_bodies();
+
 // force-kernel configuration that also returns the potential (in w)
 constexpr int kPotentialConfig = 23;
 const char *config_name(int c);

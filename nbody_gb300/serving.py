@@ -4,7 +4,7 @@
         [--n-lo 256] [--n-hi 65536] [--steps-lo 10] [--steps-hi 1000]
         [--dt 0.005] [--eps2 1e-4] [--budget-gb 120] [--slots 512]
         [--plain-sample N] [--work-budgets 2e10,1e10] [--sub-work 0]
-        [--express-n 8192] [--records PATH]
+        [--express-n 8192] [--express-ctas 32] [--newton3-min 16384] [--records PATH]
 
 Requests arrive as a Poisson process (rate per second; inf = all at t = 0),
 each with N log-uniform in [n_lo, n_hi], steps uniform in [steps_lo,
@@ -42,7 +42,7 @@ import numpy as np
 
 # device bytes of one body's resident state in the ensemble arena (FP64 x,v;
 # FP32 mass, posMass, acceleration, j-stream; split partials for up to 4)
-BYTES_PER_BODY = 6 * 8 + 4 + 16 + 16 + 16 + 8 * 16
+BYTES_PER_BODY = 6 * 8 + 4 + 16 + 16 + 16 + 8 * 16 + 3 * 8  # + FP64 Newton-3 sums
 
 
 def make_requests(n_req: int, rate: float, seed: int, n_lo: int = 256, n_hi: int = 65536,
@@ -186,7 +186,8 @@ class BatchedServer:
                  max_slots: int = 512, max_bodies: int | None = None,
                  max_ticks_per_sync: int = 32, work_budget: float = 2e10,
                  small_work: float = 1e8, sub_work: float = 0.0, express_n: int = 8192,
-                 express_ctas: int = 32, express_slots: int = 256, ensemble_factory=None):
+                 express_ctas: int = 32, express_slots: int = 256, newton3_min: int = 16384,
+                 ensemble_factory=None):
         """work_budget: interactions per step of the large requests running
         above which further large requests wait (first come first served)
         instead of joining -- about what saturates the GPU, so joining would
@@ -196,6 +197,8 @@ class BatchedServer:
         steps per tick (0: one step per tick).
         express_n: requests with N <= express_n go to the express lane
         (express_ctas CTA slots, express_slots systems); 0 = one lane.
+        newton3_min: main-lane requests with N >= newton3_min are evaluated
+        with the Newton's-third-law kernel (0: none).
         ensemble_factory(max_bodies, max_systems, eps2): the arena type
         (default nbody_gb300.Ensemble; tests pass a host-side stand-in)."""
         if ensemble_factory is None:
@@ -210,6 +213,7 @@ class BatchedServer:
             ex_budget = min(budget_bytes / 4, express_slots * express_n * BYTES_PER_BODY)
             ex = ensemble_factory(express_slots * express_n, express_slots, eps2)
             ex.set_grid(express_ctas)
+            ex.set_priority(True)  # ahead of the main lane's pending CTAs
             self.express = _Lane(ex, ex_budget, express_slots, dt, max_ticks_per_sync,
                                  work_budget, small_work, sub_work)
         main_budget = budget_bytes - ex_budget
@@ -218,6 +222,8 @@ class BatchedServer:
         ens = ensemble_factory(max_bodies, max_slots, eps2)
         if self.express is not None:
             ens.set_grid(ens.max_grid() - express_ctas)
+        if newton3_min > 0:
+            ens.set_newton3_min(newton3_min)
         self.main = _Lane(ens, main_budget, max_slots, dt, max_ticks_per_sync, work_budget,
                           small_work, sub_work)
         self.ens = ens  # the main lane's ensemble
@@ -300,9 +306,10 @@ def _pct(x, q):
 
 
 def _batched_run(reqs, eps2, dt, budget_gb, slots, work_budget=2e10, sub_work=0.0,
-                 records_out=None, express_n=8192, express_ctas=32):
+                 records_out=None, express_n=8192, express_ctas=32, newton3_min=16384):
     srv = BatchedServer(eps2, dt, budget_gb * 1e9, slots, work_budget=work_budget,
-                        sub_work=sub_work, express_n=express_n, express_ctas=express_ctas)
+                        sub_work=sub_work, express_n=express_n, express_ctas=express_ctas,
+                        newton3_min=newton3_min)
     recs, _, info = srv.run(reqs)
     srv.close()
     if records_out is not None:
@@ -318,14 +325,16 @@ def _batched_run(reqs, eps2, dt, budget_gb, slots, work_budget=2e10, sub_work=0.
             "latency_p99_s": _pct(lat, 99),
             "latency_mean_s": float(np.mean(lat)) if lat else None,
             "work_budget": work_budget, "sub_work": sub_work, "express_n": express_n,
-            "express_ctas": express_ctas, "lanes": info.get("lanes")}
+            "express_ctas": express_ctas, "newton3_min": newton3_min,
+            "lanes": info.get("lanes")}
 
 
 def serve_study(n_req: int = 20000, rates=(10.0,), seed: int = 5, n_lo: int = 256,
                 n_hi: int = 65536, steps_lo: int = 10, steps_hi: int = 1000, dt: float = 0.005,
                 eps2: float = 1e-4, budget_gb: float = 120.0, slots: int = 512,
                 plain_sample: int | None = None, work_budgets=(2e10,), sub_work: float = 0.0,
-                records_out=None, express_n: int = 8192, express_ctas: int = 32) -> dict:
+                records_out=None, express_n: int = 8192, express_ctas: int = 32,
+                newton3_min: int = 16384) -> dict:
     """Both servers on the same stream at each arrival rate.  The plain
     server's per-request service times are measured once (they do not depend
     on the arrival times) and replayed through the FIFO rule at every rate.
@@ -357,7 +366,7 @@ def serve_study(n_req: int = 20000, rates=(10.0,), seed: int = 5, n_lo: int = 25
     for rate in rates:
         reqs = make_requests(n_req, rate, seed, n_lo, n_hi, steps_lo, steps_hi)
         runs = [_batched_run(reqs, eps2, dt, budget_gb, slots, wb, sub_work, records_out,
-                             express_n, express_ctas) for wb in work_budgets]
+                             express_n, express_ctas, newton3_min) for wb in work_budgets]
         b = runs[0]
         arrivals = [r["arrival"] for r in reqs]
         pfin = fifo_finish_times(arrivals, service)
@@ -398,6 +407,8 @@ def main(argv=None):
                     help="requests with N <= this run in the express lane (0: one lane)")
     ap.add_argument("--express-ctas", type=int, default=32,
                     help="CTA slots of the express lane's persistent force launch")
+    ap.add_argument("--newton3-min", type=int, default=16384,
+                    help="main-lane requests with N >= this use the Newton-3 kernel (0: none)")
     ap.add_argument("--records", default=None,
                     help="write every batched request's record (JSON) to this path")
     a = ap.parse_args(argv)
@@ -406,7 +417,7 @@ def main(argv=None):
     recs = [] if a.records else None
     r = serve_study(a.requests, rates, a.seed, a.n_lo, a.n_hi, a.steps_lo, a.steps_hi, a.dt,
                     a.eps2, a.budget_gb, a.slots, a.plain_sample, budgets, a.sub_work, recs,
-                    a.express_n, a.express_ctas)
+                    a.express_n, a.express_ctas, a.newton3_min)
     if a.records:
         with open(a.records, "w") as f:
             json.dump(recs, f)

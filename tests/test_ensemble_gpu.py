@@ -214,3 +214,43 @@ def test_substeps_give_identical_results_and_fewer_ticks(cuda):
     e.close()
     for n, steps, sub in cases:
         assert done_at[n] == 1 + -(-steps // sub), (n, done_at[n])
+
+
+def test_newton3_systems_in_the_ensemble(cuda):
+    """Systems at or above the Newton-3 threshold are evaluated with the
+    Newton's-third-law kernel beside work-queue systems: their first forces
+    match FP64 like the others, and 20 KDK steps agree with the
+    single-system Newton-3 path to FP64-order rounding."""
+    e = nb.Ensemble(40000, 8, EPS2)
+    e.set_newton3_min(4096)
+    sizes = [3000, 5000, 9000, 2100, 4096]
+    slots, pms = {}, {}
+    for n in sizes:
+        p, v, m, pm = _ball(n, 300 + n)
+        slots[n] = e.add(p, v, m, 0.002, 20)
+        pms[n] = pm
+    e.tick(1)  # initial accelerations only
+    e.synchronize()
+    assert nb.last_status() == 0
+    for n in sizes:
+        _, _, a = e.get_state(slots[n])
+        assert O.per_body_rel_error(a, _f64(pms[n]))[0] <= TOL_VS_FP64, n
+    e.tick(20)
+    e.synchronize()
+    assert sorted(e.finished()) == sorted(slots.values())
+    for n in (5000, 9000):
+        pe, ve, _ = e.get_state(slots[n])
+        p, v, m, _ = _ball(n, 300 + n)
+        s = nb.System(n, nb.INTEGRATOR_KDK64, EPS2, 0.002, 1.0)
+        s.set_force_algorithm("newton3")
+        s.set_state64(p, v, m)
+        s.step(20)
+        ps, vs = s.get_state64()
+        s.close()
+        assert np.abs(pe - ps).max() <= 1e-9 * np.abs(ps).max(), n
+        # v starts at 0 and is the sum of 20 dt-weighted FP32 forces, whose
+        # FP64 summation order may differ by an FP32 ulp between the runs
+        _, _, a = e.get_state(slots[n])
+        bound = 4 * 20 * 0.002 * np.abs(a[:, :3]).max() * 2.0 ** -23
+        assert np.abs(ve - vs).max() <= bound, n
+    e.close()

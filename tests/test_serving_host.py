@@ -53,6 +53,12 @@ class FakeEnsemble:
         assert 0 < ctas <= self.grid_max
         self.grid = ctas
 
+    def set_newton3_min(self, nmin):
+        self.newton3_min = nmin
+
+    def set_priority(self, high):
+        self.high_priority = bool(high)
+
     def add(self, p, v, m, dt, steps):
         free = [s for s in range(self.max_systems) if s not in self.sys]
         bodies = sum(x["n"] for x in self.sys.values()) + p.shape[0]
@@ -111,6 +117,7 @@ def _reqs(ns, steps=20):
 def test_lanes_route_by_size():
     srv = _server(budget_bytes=4e9, express_n=1000, express_ctas=32)
     assert srv.ens.grid == 304 - 32 and srv.express.ens.grid == 32
+    assert srv.express.ens.high_priority and srv.ens.newton3_min == 16384
     reqs = _reqs([300, 5000, 800, 2000, 1000, 1001])
     recs, _, info = srv.run(reqs)
     assert all("latency" in r for r in recs.values())
