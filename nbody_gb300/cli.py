@@ -11,8 +11,11 @@ reference's output (scripts/nbody-stats.py) read this one too.  The bodies
 are the reference driver's own initial conditions (randomUnitBodies, scale
 0.9, velocity scale 8, src/nbody.cu:996), N = --bodies x 1024, softening 0.1
 (eps2 0.01), timestep 0.016, damping 0.95 (src/nbody.cu:151-156) unless
-overridden.  The one algorithm row, GPU_GB300, runs the device-resident step
-loop; the printed milliseconds are the force launch's CUDA-event time, as the
+overridden.  Two algorithm rows run the device-resident step loop:
+GPU_GB300 (the one-sided force kernel) and GPU_GB300_Newton3 (each pair
+once); --cycle-after moves to the next row every N steps and an iteration
+is one pass through the rows, as in the reference (src/nbody.cu:1055-1068).
+The printed milliseconds are the force launch's CUDA-event time, as the
 reference prints its algorithm's own timing.  The crosscheck compares each
 step's forces with an FP64 all-pairs sum on the host (the reference compares
 with its FP32 CPU_SOA) using the reference's relError metric.
@@ -23,7 +26,8 @@ import argparse
 import sys
 import time
 
-ALGORITHMS = ["GPU_GB300"]
+ALGORITHMS = ["GPU_GB300", "GPU_GB300_Newton3"]
+FORCE_ALGORITHM = {"GPU_GB300": "onesided", "GPU_GB300_Newton3": "newton3"}
 
 
 def _gpu_count() -> int:
@@ -140,7 +144,9 @@ def main(argv=None) -> int:
                       pm[:, 3].copy())
     s.set_timing(True)
     width = max(len(x) for x in ALGORITHMS)
-    name = ALGORITHMS[resolve_algorithm(a.algorithm)]
+    alg = resolve_algorithm(a.algorithm)
+    name = ALGORITHMS[alg]
+    s.set_force_algorithm(FORCE_ALGORITHM[name])
     steps = iterations = 0
     last = time.monotonic()
     idx = np.arange(n)
@@ -162,7 +168,12 @@ def main(argv=None) -> int:
         steps += 1
         if a.cycle_after and steps % a.cycle_after == 0:
             steps = 0
-            iterations += 1  # one algorithm: cycling wraps to the start
+            alg += 1
+            if alg == len(ALGORITHMS):  # wrapped: one pass through the rows
+                alg = 0
+                iterations += 1
+            name = ALGORITHMS[alg]
+            s.set_force_algorithm(FORCE_ALGORITHM[name])
         elif not a.cycle_after:
             iterations += 1
         if a.iterations and iterations >= a.iterations:

@@ -36,6 +36,11 @@ def test_flag_errors_and_list():
     assert _run("--algorithm", "NoSuchAlgorithm").returncode == 1
     r = _run("--list")
     assert r.returncode == 0 and "0 - GPU_GB300" in r.stdout
+    assert "1 - GPU_GB300_Newton3" in r.stdout
+    from nbody_gb300 import cli
+    assert cli.resolve_algorithm("GPU_GB300") == 0
+    assert cli.resolve_algorithm("gpu_gb300_newton3") == 1
+    assert cli.resolve_algorithm("1") == 1 and cli.resolve_algorithm("2") is None
 
 
 @pytest.mark.gpu
@@ -49,3 +54,16 @@ def test_cli_runs_and_reports(cuda):
         assert m and float(m.group("ms")) > 0
         assert float(m.group("error")) < 1e-2  # per-component relError vs FP64
     assert "Running simulation with 2048 particles, crosscheck enabled" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cli_cycles_through_both_rows(cuda):
+    """--cycle-after 2 --iterations 1: two steps of each row, as the
+    reference's driver cycles its algorithm table."""
+    r = _run("--bodies", "2", "--iterations", "1", "--cycle-after", "2", "--verbose")
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.replace("\r", "\n").splitlines() if l.strip()]
+    names = [LINE_RE.search(l).group("algorithm").strip() for l in lines]
+    assert names == ["GPU_GB300"] * 2 + ["GPU_GB300_Newton3"] * 2
+    for l in lines:
+        assert float(LINE_RE.search(l).group("error")) < 1e-2
