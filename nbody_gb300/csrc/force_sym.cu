@@ -5,7 +5,10 @@
 //
 // Here the unit of work is a block pair (bi, bj), bi <= bj, of 2048-body
 // blocks, one CTA of 8 warps each (one CTA per SM: up to 255 registers a
-// thread, spent on independent work per warp rather than on more warps):
+// thread, spent on independent work per warp rather than on more warps;
+// sizes whose pairs would not fill the GPU use 1024-body blocks with 4
+// targets and 4 sources per lane, 2 CTAs per SM -- the same scheme at half
+// the width):
 //   * warp w holds 256 targets of block bi in registers (8 per lane, negated
 //     and duplicated into f32x2 pairs, with their masses);
 //   * block bj is visited as 8 source sets of 256 bodies; every lane loads 8
@@ -43,15 +46,24 @@ namespace sym {
 
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
-constexpr int KI = 8;                        // targets per lane
-constexpr int KJ = 8;                        // sources per lane (4 f32x2 pairs)
-constexpr int NC = KJ / 2;                   // f32x2 source pairs per lane
-constexpr int kMinBlocks = 1;                // resident CTAs per SM (register cap)
-constexpr int kSet = 32 * KJ;                // sources per set
-constexpr int kBlock = kWarps * 32 * KI;     // bodies per block (1024)
-static_assert(kBlock == kWarps * kSet, "a block is 8 source sets");
-constexpr int kFoldSets = kSet >= 256 ? 1 : 256 / kSet;  // sets per compensated fold
-static_assert(kWarps % kFoldSets == 0, "folds end with the block's last set");
+
+// Geometry: KI targets and KJ = KI sources per lane.  KI = 8: 2048-body
+// blocks, one CTA per SM (up to 255 registers); KI = 4: 1024-body blocks,
+// two CTAs per SM (128 registers), four times the block pairs for sizes
+// whose 2048-body pairs would not fill the GPU.
+template <int KI_>
+struct Geo {
+    static constexpr int KI = KI_;                  // targets per lane
+    static constexpr int KJ = KI_;                  // sources per lane
+    static constexpr int NC = KJ / 2;               // f32x2 source pairs per lane
+    static constexpr int kMinBlocks = KI_ >= 8 ? 1 : 2;  // resident CTAs per SM
+    static constexpr int kSet = 32 * KJ;            // sources per set
+    static constexpr int kBlock = kWarps * 32 * KI; // bodies per block
+    static constexpr int kFoldSets = kSet >= 256 ? 1 : 256 / kSet;  // sets per fold
+    static_assert(kBlock == kWarps * kSet, "a block is 8 source sets");
+    static_assert(kWarps % kFoldSets == 0, "folds end with the block's last set");
+};
+constexpr int kWideKI = 8, kNarrowKI = 4;
 
 struct Params {
     const float4 *__restrict__ pm;  // AOS posMass (targets), n bodies
@@ -83,7 +95,7 @@ __device__ __forceinline__ void pair_of(long long p, int nb, int &bi, int &bj) {
 // 32 rotation steps over one source set.  REACT: also accumulate the
 // sources' reactions (both sides); otherwise only the targets' sums.  The
 // branch on REACT is resolved at compile time, outside the step loop.
-template <bool REACT>
+template <bool REACT, int KI, int NC = KI / 2>
 __device__ __forceinline__ void rotate_set(f2 (&sx)[NC], f2 (&sy)[NC], f2 (&sz)[NC],
                                            f2 (&sm)[NC], f2 (&rx)[NC], f2 (&ry)[NC],
                                            f2 (&rz)[NC],
@@ -137,7 +149,11 @@ __device__ __forceinline__ void rotate_set(f2 (&sx)[NC], f2 (&sy)[NC], f2 (&sz)[
 }
 
 // One block pair (bi, bj) of one system, by the whole CTA.
+template <int KI_>
 __device__ __forceinline__ void sym_block_pair(const Params &P, int bi, int bj) {
+    using G = Geo<KI_>;
+    constexpr int KI = G::KI, KJ = G::KJ, NC = G::NC, kSet = G::kSet, kBlock = G::kBlock,
+                  kFoldSets = G::kFoldSets;
     __shared__ float red[kWarps][3][kSet];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool diag = (bi == bj);
@@ -179,9 +195,11 @@ __device__ __forceinline__ void sym_block_pair(const Params &P, int bi, int bj) 
             rx[c] = ry[c] = rz[c] = zero2;
         }
         if (mode == 2)
-            rotate_set<true>(sx, sy, sz, sm, rx, ry, rz, nx, ny, nz, nm, ax, ay, az, eps2p, lane);
+            rotate_set<true, KI>(sx, sy, sz, sm, rx, ry, rz, nx, ny, nz, nm, ax, ay, az, eps2p,
+                                 lane);
         else if (mode == 1)
-            rotate_set<false>(sx, sy, sz, sm, rx, ry, rz, nx, ny, nz, nm, ax, ay, az, eps2p, lane);
+            rotate_set<false, KI>(sx, sy, sz, sm, rx, ry, rz, nx, ny, nz, nm, ax, ay, az, eps2p,
+                                  lane);
         // fold target sums into the compensated sums every 256 sources
         if ((s + 1) % kFoldSets == 0) {
 #pragma unroll
@@ -235,16 +253,17 @@ __device__ __forceinline__ void sym_block_pair(const Params &P, int bi, int bj) 
     }
 }
 
-__global__ void __launch_bounds__(kThreads, kMinBlocks) sym_kernel(Params P) {
+template <int KI_>
+__global__ void __launch_bounds__(kThreads, Geo<KI_>::kMinBlocks) sym_kernel(Params P) {
     int bi, bj;
     pair_of(blockIdx.x, P.nblocks, bi, bj);
-    sym_block_pair(P, bi, bj);
+    sym_block_pair<KI_>(P, bi, bj);
 }
 
 // Many systems in one launch (the ensemble's Newton-3 systems): CTA b takes
 // block pair b - pair_begin[s] of the system s whose range holds b (binary
 // search over the systems' prefix counts).
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
+__global__ void __launch_bounds__(kThreads, Geo<kWideKI>::kMinBlocks)
     sym_systems_kernel(const SymSystem *__restrict__ tab, int nsys) {
     const long long b = blockIdx.x;
     int lo = 0, hi = nsys - 1;
@@ -266,7 +285,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     P.eps2 = t.eps2;
     int bi, bj;
     pair_of(b - t.pair_begin, t.nblocks, bi, bj);
-    sym_block_pair(P, bi, bj);
+    sym_block_pair<kWideKI>(P, bi, bj);
 }
 
 // FP64 sums -> FP32 accelerations {ax, ay, az, 0}, and the sums zeroed for
@@ -306,21 +325,42 @@ int launch_sym_systems(const SymSystem *d_tab, const SymSystem *h_tab, int nsys,
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
-int sym_block_bodies() { return sym::kBlock; }
+int sym_block_bodies() { return sym::Geo<sym::kWideKI>::kBlock; }
 
 }  // namespace nbgb
 
 namespace {
 
 struct SymLayout {
+    int ki, block;  // geometry: targets per lane, bodies per block
     int nblocks, npad;
     size_t off_js, off_acc, bytes;
 };
 
+int device_sms() {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms <= 0) {
+        cudaGetLastError();  // no device: plan for a 152-SM GB300
+        sms = 152;
+    }
+    return sms;
+}
+
+// The wide geometry (2048-body blocks, one CTA per SM) when its block pairs
+// give every SM at least two; the narrow one (1024-body blocks, four times
+// the pairs) below that.
 SymLayout sym_layout(size_t n) {
+    using Wide = nbgb::sym::Geo<nbgb::sym::kWideKI>;
+    using Narrow = nbgb::sym::Geo<nbgb::sym::kNarrowKI>;
     SymLayout L;
-    L.nblocks = (int)((n + nbgb::sym::kBlock - 1) / nbgb::sym::kBlock);
-    L.npad = L.nblocks * nbgb::sym::kBlock;
+    const long long nbw = (long long)((n + Wide::kBlock - 1) / Wide::kBlock);
+    const bool wide = nbw * (nbw + 1) / 2 >= 2LL * device_sms();
+    L.ki = wide ? Wide::KI : Narrow::KI;
+    L.block = wide ? Wide::kBlock : Narrow::kBlock;
+    L.nblocks = (int)((n + L.block - 1) / L.block);
+    L.npad = L.nblocks * L.block;
     L.off_js = 0;
     L.off_acc = ((size_t)L.npad * 16 + 255) / 256 * 256;
     L.bytes = L.off_acc + (size_t)3 * L.npad * sizeof(double);
@@ -354,7 +394,7 @@ NBGB_API int nbgb_force_newton3(float *force, const float *posMass, float soften
     nbgb::ForcePlan pl;
     pl.n = N;
     pl.ntiles = L.nblocks;
-    pl.tile_bodies = nbgb::sym::kBlock;
+    pl.tile_bodies = L.block;
     pl.js_vpb = 1;
     pl.nsplit = 1;
     pl.off_js = L.off_js;
@@ -375,7 +415,11 @@ NBGB_API int nbgb_force_newton3(float *force, const float *posMass, float soften
     const long long pairs = (long long)L.nblocks * (L.nblocks + 1) / 2;
     if (pairs > (1ll << 31) - 1)
         return NBGB_ERR_TOO_LARGE;
-    nbgb::sym::sym_kernel<<<(unsigned)pairs, nbgb::sym::kThreads, 0, st>>>(P);
+    if (L.ki == nbgb::sym::kWideKI)
+        nbgb::sym::sym_kernel<nbgb::sym::kWideKI><<<(unsigned)pairs, nbgb::sym::kThreads, 0, st>>>(P);
+    else
+        nbgb::sym::sym_kernel<nbgb::sym::kNarrowKI>
+            <<<(unsigned)pairs, nbgb::sym::kThreads, 0, st>>>(P);
     nbgb::sym::sym_finish_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(
         acc, (int)N, L.npad, (float4 *)force);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
