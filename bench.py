@@ -11,16 +11,24 @@ included, the reference's convention, src/nbody.cu:1026) and 20 FLOP per
 interaction (src/nbody.cu:1027).
 
   value     device-timed: sum of per-step CUDA-event times on the system's
-            stream, L2 flushed (256 MiB write) between steps outside the events
+            stream, L2 flushed (a 256 MiB read, which leaves no dirty lines
+            behind) between steps outside the events
   e2e       the reference-facing drop-in ComputeGravitation_GPU_GB300 with
             HOST buffers: per step pinned H2D of posMass, the call, D2H of the
             forces, all inside a host-clock timed region
   roofline  the force kernel: 20 N^2 FLOP / its CUDA-event launch time, over
             the FP32 pipe peak measured by the library's FMA microbenchmark
-            on this GPU (max of scalar and f32x2), plus the MUFU ceiling
+            on this GPU (max of scalar and f32x2), plus the MUFU ceiling;
+            `integrate` holds the same for the two HBM-bound FP64 integrate
+            kernels (algorithmic bytes / CUDA-event time over the measured
+            copy bandwidth)
   cpu_baseline  the oracle's restatement of the reference's CPU_SOA loop
             (OpenMP, all host threads) on a bounded sample of target bodies
             against all N sources
+  accuracy  the drop-in's forces of the e2e leg on a seeded 1,024-body
+            sample, per body against the FP64 all-pairs sum and against the
+            oracle's CPU_AOS restatements (IEEE and the reference's flags),
+            computed outside every timed region
 
 --impl reference times the reference's CPU implementation of the path (the
 reference's own compiled CPU_SOA when oracle/_ref was built on this machine,
@@ -173,34 +181,49 @@ def cpu_rate(pm: np.ndarray, seconds: float):
     info = {"kind": "port", "cores": impl.num_threads(),
             "sample": f"{ni} target bodies x {n} sources of the same Plummer system "
                       f"({ni * n:.3e} interactions, {el:.1f} s), oracle restatement of "
-                      "CPU_SOA (src/nbody_CPU_SOA.cpp:53-105) built with the reference's "
-                      "flags (-O3 -ffast-math -fopenmp)"}
+                      f"CPU_SOA (src/nbody_CPU_SOA.cpp:53-105) built with {O.fast_flags()} "
+                      "(the reference's flags, meson.build:33-58)"}
     return rate, el, info
 
 
+TRAFFIC_TABLE = os.path.join(ROOT, "nbody_gb300", "tuning", "force_dram_traffic.json")
+# measured copy bandwidth of this GPU type when MEASURED_PEAKS.json is absent
+HBM_FALLBACK_GBS = 6800.0
+
+
 def profiled_traffic(config_name: str, n: int, nsplit: int):
-    """DRAM bytes per force launch from the committed ncu summary, when it was
-    captured for this kernel configuration, N and j-split (else None)."""
-    path = os.path.join(ROOT, "profiles", "force_kernel_n1048576_dram.md")
-    if not os.path.exists(path):
+    """DRAM bytes per force launch measured by ncu for this kernel
+    configuration, N and j-split (nbody_gb300/tuning/force_dram_traffic.json),
+    else None."""
+    try:
+        table = json.load(open(TRAFFIC_TABLE))
+    except (OSError, ValueError):
         return None
-    import re
-    for line in open(path):
-        m = re.match(r"traffic_bytes_per_launch:\s*(\d+)\s+config\s+(\S+)\s+n\s+(\d+)"
-                     r"\s+nsplit\s+(\d+)", line.strip())
-        if m and m.group(2) == config_name and int(m.group(3)) == n and \
-                int(m.group(4)) == nsplit:
-            return int(m.group(1))
+    for e in table.get("entries", []):
+        if e["config"] == config_name and e["n"] == n and e["nsplit"] == nsplit:
+            return int(e["bytes_per_launch"])
     return None
 
 
+def hbm_peak():
+    """(GB/s, source): the measured copy bandwidth, else the fallback."""
+    try:
+        v = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        return v, "measured (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"
+    except (OSError, ValueError, KeyError, TypeError):
+        return HBM_FALLBACK_GBS, "fallback (6.8 TB/s, one earlier GB300 measurement)"
+
+
 def run_reference_arm(args, ws, rank):
+    """The reference's CPU path alone: the oracle's restatement of CPU_SOA
+    built with the reference's flags, on inputs from the oracle's restatement
+    of the Plummer generator (byte-identical to the library's, tested), so
+    this arm loads no GB300 code."""
     if rank != 0:
         return
-    import nbody_gb300 as nb
     from oracle import oracle as O
     O.build(ref=False)
-    _, _, pm, _ = nb.ic_plummer(N_BODIES, SEED)
+    _, _, pm = O.ieee().ic_plummer(N_BODIES, SEED)
     impl = O.fast()
     run = impl.soa_timer(pm, EPS2)
     t0 = time.perf_counter()
@@ -231,10 +254,11 @@ def run_reference_arm(args, ws, rank):
                          "kind": "port",
                          "sample": f"{ni} targets x {N_BODIES} sources per step "
                                    f"({ni * N_BODIES:.3e} interactions), oracle restatement "
-                                   "of the reference's CPU_SOA with its build flags (the "
-                                   "reference's own CPU objects are built only where its "
-                                   "sources are present; tests check the restatement "
-                                   "against them)"},
+                                   "of the reference's CPU_SOA (src/nbody_CPU_SOA.cpp:53-105) "
+                                   f"built with {O.fast_flags()} (the reference's flags, "
+                                   "meson.build:33-58; its own CPU objects are built only "
+                                   "where its sources are present, and tests check the "
+                                   "restatement against them)"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -266,7 +290,7 @@ def run_gb300(args, ws, rank, local):
         sysm.set_force_algorithm("newton3")
     sysm.set_timing(True)
     stream = torch.cuda.ExternalStream(sysm.stream, device=dev)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    flush = L2Flush(dev)
 
     for _ in range(args.warmup):
         sysm.step(1)
@@ -274,7 +298,7 @@ def run_gb300(args, ws, rank, local):
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    force_ms = []
+    force_ms, kd_ms, hk_ms = [], [], []
     clocks = Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
                     if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local)
     _barrier(ws)
@@ -283,11 +307,14 @@ def run_gb300(args, ws, rank, local):
     wall0 = time.perf_counter()
     for k in range(args.steps):
         with torch.cuda.stream(stream):
-            flush.zero_()  # evict L2 between steps (outside the events)
+            flush()  # evict L2 between steps (outside the events)
             ev[k][0].record(stream)
         sysm.step(1)
         ev[k][1].record(stream)
         force_ms.append(sysm.last_force_ms())
+        a, b = sysm.last_integrate_ms()
+        kd_ms.append(a)
+        hk_ms.append(b)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
@@ -303,6 +330,7 @@ def run_gb300(args, ws, rank, local):
     cfg_name = nb.force_config_names()[cfg] if args.force == 'onesided' else 'newton3'
     traffic = profiled_traffic(cfg_name, n, nsplit)
     sysm.close()
+    integrate = integrate_roofline(n, kd_ms, hk_ms)
 
     # e2e: the drop-in entry point with host buffers
     pm_h = torch.from_numpy(pm_np).pin_memory()
@@ -336,19 +364,20 @@ def run_gb300(args, ws, rank, local):
                                "FP64 KDK integrate, eps2=1e-4, dt=0.005",
                    "n_bodies": n, "integrator": "kdk64", "force_config": cfg_name,
                    "nsplit": nsplit,
-                   "l2": "flushed between steps (256 MiB write outside the step events)",
+                   "l2": "flushed between steps (256 MiB read outside the step events)",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fp32_peak / 1e12,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
                      "traffic_unit": "bytes per launch (ncu dram read+write, "
-                                     "profiles/force_kernel_n1048576_dram.md)",
+                                     "nbody_gb300/tuning/force_dram_traffic.json)",
                      "algorithmic_bytes": 48 * n,  # read targets + sources, write forces
                      "peak_source": "measured on this GPU by nbgb_measure_peak "
                                     f"(FFMA {ffma / 1e12:.2f}, FFMA2 {ffma2 / 1e12:.2f} "
                                     "TFLOP/s; FMA = 2 FLOP)",
                      "kernel_ms": kernel_ms,
                      "mufu_peak_per_s": mufu,
-                     "mufu_frac": (float(n) * float(n) / (kernel_ms * 1e-3)) / mufu},
+                     "mufu_frac": (float(n) * float(n) / (kernel_ms * 1e-3)) / mufu,
+                     "integrate": integrate},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": n * 16},
         "gpu_launches": 3 * args.steps,
@@ -361,8 +390,73 @@ def run_gb300(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         rate, el, info = cpu_rate(pm_np, args.cpu_seconds)
         line["cpu_baseline"] = dict(value=rate, unit=UNIT, **info)
+        line["accuracy"] = force_accuracy(pm_np, f_h.numpy())
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+class L2Flush:
+    """Evicts L2 (129 MB on GB300) by reading a 256 MiB buffer: a read leaves
+    clean lines, so the next kernel pays no write-back of the flush itself."""
+
+    def __init__(self, dev):
+        import torch
+        self.buf = torch.ones(64 << 20, dtype=torch.int32, device=dev)
+
+    def __call__(self):
+        self.buf.amax()
+
+
+# bytes each FP64 integrate kernel moves per body (algorithmic: every array
+# read and written once)
+KICK_DRIFT_BYTES = 148  # read x, v (48), a (16), m (4); write x, v (48), posMass, j-stream (32)
+HALF_KICK_BYTES = 64    # read v (24), a (16); write v (24)
+
+
+def integrate_roofline(n, kd_ms, hk_ms):
+    """HBM roofline of the two FP64 integrate kernels from their per-step
+    CUDA-event times (each step runs right after the L2 flush, so the
+    kick+drift reads cold state)."""
+    peak, src = hbm_peak()
+    out = {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": src}
+    for name, per_body, ms in (("kick_drift", KICK_DRIFT_BYTES, kd_ms),
+                               ("half_kick", HALF_KICK_BYTES, hk_ms)):
+        t = float(np.median(ms)) if ms else 0.0
+        gbs = per_body * float(n) / (t * 1e-3) / 1e9 if t > 0 else None
+        out[name] = {"bytes_per_body": per_body, "bytes": per_body * n, "ms": t,
+                     "achieved": gbs, "frac": gbs / peak if gbs else None}
+    return out
+
+
+def force_accuracy(pm: np.ndarray, force: np.ndarray, k: int = 1024, seed: int = 7):
+    """Per-body |F - T| / |T| of `force` on a seeded sample of k bodies: T the
+    FP64 all-pairs sum of the same FP32 inputs, and the CPU_AOS restatement
+    (src/nbody_CPU_AOS.cpp:51-98) built IEEE (sequential sum) and with the
+    reference's flags.  The reference-flag build is also given net of its
+    own distance from FP64 (its aarch64 reciprocal square root is
+    low-precision)."""
+    from oracle import oracle as O
+    n = pm.shape[0]
+    idx = np.random.default_rng(seed).choice(n, min(k, n), replace=False)
+    f = np.asarray(force, np.float64)[idx, :3]
+    t64 = O.ieee().forces_f64(pm, float(np.float32(EPS2)), idx)
+
+    def stats(ref):
+        d = np.linalg.norm(f - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        return {"max": float(d.max()), "rms": float(np.sqrt(np.mean(d * d)))}
+
+    ieee = O.ieee().forces_aos_idx(pm, EPS2, idx)[:, :3].astype(np.float64)
+    fast = O.fast().forces_aos_idx(pm, EPS2, idx)[:, :3].astype(np.float64)
+    net = (np.linalg.norm(f - fast, axis=1) - np.linalg.norm(fast - t64, axis=1)) / \
+        np.linalg.norm(fast, axis=1)
+    return {"sample": f"{idx.size} seeded bodies of the N={n:,} input, forces of the "
+                      "drop-in call (e2e leg)",
+            "vs_fp64": stats(t64), "vs_cpu_aos_ieee": stats(ieee),
+            "vs_cpu_aos_reference_flags": dict(stats(fast),
+                                               net_of_own_fp64_distance_max=float(
+                                                   max(0.0, net.max())),
+                                               flags=O.fast_flags()),
+            "gates": {"vs_reference_max": 1e-5, "vs_fp64_max": 5e-6}}
 
 
 def measure_newton3(args, n, p3, v3, pm_np, dev, ffma, ffma2, fp32_peak, flush):
@@ -384,7 +478,7 @@ def measure_newton3(args, n, p3, v3, pm_np, dev, ffma, ffma2, fp32_peak, flush):
     fms = []
     for k in range(args.steps):
         with torch.cuda.stream(stream):
-            flush.zero_()
+            flush()
             ev[k][0].record(stream)
         s.step(1)
         ev[k][1].record(stream)

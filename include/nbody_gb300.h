@@ -58,7 +58,10 @@ NBGB_API float ComputeGravitation_GPU_GB300(float *force, float *posMass, float 
 NBGB_API float ComputeGravitation_GPU_GB300_Newton3(float *force, float *posMass,
                                                     float softeningSquared, size_t N);
 
-/* Frees the drop-in entry point's cached scratch space on every device. */
+/* Frees the drop-in entry point's cached scratch space on every device.
+   Scratch cached in a context that has since been reset (cudaDeviceReset)
+   is forgotten, not freed: the reset released it, and the next call
+   allocates afresh. */
 NBGB_API void nbgb_release_workspace(void);
 
 /* ======================================================================== */
@@ -150,17 +153,34 @@ NBGB_API size_t nbgb_force_static_capacity_bytes(void);
 NBGB_API int nbgb_integrate_reference(float *posMass, float *velInvMass, const float *force,
                                       float dt, float damping, size_t N, void *stream);
 
+/*
+ * Replaces: the same step as the reference binary computes it.  Built with
+ * its own flags (meson.build:33-38: -O3 -ffast-math -march=native), GCC
+ * contracts the position update of integrateOne (src/nbody.cu:178-181) into
+ * one fused multiply-add and keeps the velocity update as written.
+ * fused_drift = 1 reproduces that (x = fma(v, dt, x)), bit-identical to the
+ * reference's compiled integrateGravitation_SOA; fused_drift = 0 is
+ * nbgb_integrate_reference.
+ */
+NBGB_API int nbgb_integrate_reference_ex(float *posMass, float *velInvMass, const float *force,
+                                         float dt, float damping, size_t N, int fused_drift,
+                                         void *stream);
+
 /* ======================================================================== */
 /* Device-resident simulation (the reference's per-step orchestration,      */
 /* src/nbody.cu:293-470, without host copies)                               */
 /* ======================================================================== */
 
-#define NBGB_INTEGRATOR_REFERENCE 0 /* integrateOne, FP32, damping        */
-#define NBGB_INTEGRATOR_KDK64 1     /* FP64 kick-drift-kick, a = F         */
+#define NBGB_INTEGRATOR_REFERENCE 0       /* integrateOne, FP32, damping       */
+#define NBGB_INTEGRATOR_KDK64 1           /* FP64 kick-drift-kick, a = F        */
+#define NBGB_INTEGRATOR_REFERENCE_FUSED 2 /* integrateOne with x = fma(v,dt,x),
+                                             as the reference binary computes */
 
 typedef struct nbgb_system nbgb_system;
 
-/* Allocates all device state on the current device; NULL on failure. */
+/* Allocates all device state on the current device; NULL on failure.  A
+   system (and an ensemble, below) belongs to the CUDA context it was created
+   in: destroy it before a cudaDeviceReset. */
 NBGB_API nbgb_system *nbgb_system_create(size_t N, int integrator, float softeningSquared,
                                          float dt, float damping);
 NBGB_API void nbgb_system_destroy(nbgb_system *sys);
@@ -176,10 +196,15 @@ NBGB_API int nbgb_system_step(nbgb_system *sys, int nsteps);
 NBGB_API int nbgb_system_set_graph(nbgb_system *sys, int enable);
 /* 0: one-sided force kernel (default); 1: Newton's-third-law variant. */
 NBGB_API int nbgb_system_set_force_algorithm(nbgb_system *sys, int algorithm);
-/* Bracket every force launch with CUDA events on the system's stream (steps
-   then run eagerly); nbgb_system_last_force_ms reads the latest one. */
+/* Bracket every force launch and every integrate launch with CUDA events on
+   the system's stream (steps then run eagerly); nbgb_system_last_force_ms
+   reads the latest force launch, nbgb_system_last_integrate_ms the latest
+   integrate launches: step_ms the reference integrate or the FP64
+   kick+drift, half_kick_ms the closing FP64 half kick (0 if none ran). */
 NBGB_API int nbgb_system_set_timing(nbgb_system *sys, int enable);
 NBGB_API int nbgb_system_last_force_ms(nbgb_system *sys, float *ms);
+NBGB_API int nbgb_system_last_integrate_ms(nbgb_system *sys, float *step_ms,
+                                           float *half_kick_ms);
 NBGB_API int nbgb_system_synchronize(nbgb_system *sys);
 /* HOST float4 arrays out (either may be NULL); synchronises. */
 NBGB_API int nbgb_system_get_state(nbgb_system *sys, float *posMass, float *velInvMass);

@@ -28,6 +28,7 @@ from ._lib import LIB_PATH, NbgbError, check, load  # noqa: F401
 
 INTEGRATOR_REFERENCE = 0
 INTEGRATOR_KDK64 = 1
+INTEGRATOR_REFERENCE_FUSED = 2  # x = fma(v, dt, x), as the reference binary computes it
 
 # Reference driver constants (src/nbody.cu:80-81, 151-156).
 REFERENCE_SOFTENING = 0.1
@@ -157,12 +158,15 @@ def force_newton3(posMass, softeningSquared: float, out=None, stream=None,
     return out
 
 
-def integrate_reference(posMass, velInvMass, force_, dt: float, damping: float, stream=None):
-    """In place on (N,4) float32 CUDA tensors (src/nbody.cu:158-182)."""
+def integrate_reference(posMass, velInvMass, force_, dt: float, damping: float, stream=None,
+                        fused_drift: bool = False):
+    """In place on (N,4) float32 CUDA tensors (src/nbody.cu:158-182); with
+    fused_drift the position update is one fused multiply-add, as the
+    reference binary built with its own flags computes it."""
     n = posMass.shape[0]
-    check(load().nbgb_integrate_reference(_dev(posMass), _dev(velInvMass), _dev(force_), dt,
-                                          damping, n, _stream(stream)),
-          "nbgb_integrate_reference")
+    check(load().nbgb_integrate_reference_ex(_dev(posMass), _dev(velInvMass), _dev(force_), dt,
+                                             damping, n, int(fused_drift), _stream(stream)),
+          "nbgb_integrate_reference_ex")
 
 
 def measure_peak(which: str, iters: int = 4096, reps: int = 5):
@@ -247,6 +251,15 @@ class System:
         ms = ctypes.c_float()
         check(self.lib.nbgb_system_last_force_ms(self.h, ctypes.byref(ms)), "last_force_ms")
         return ms.value
+
+    def last_integrate_ms(self):
+        """(step_ms, half_kick_ms) of the latest timed integrate launches:
+        the reference integrate or the FP64 kick+drift, and the closing FP64
+        half kick (0.0 when none ran)."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        check(self.lib.nbgb_system_last_integrate_ms(self.h, ctypes.byref(a), ctypes.byref(b)),
+              "last_integrate_ms")
+        return a.value, b.value
 
     def get_state(self):
         pm = np.zeros((self.n, 4), np.float32)

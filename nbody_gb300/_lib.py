@@ -42,6 +42,8 @@ SIGNATURES = {
     "nbgb_force_static_capacity_bytes": (c_size, []),
     "nbgb_integrate_reference": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_float,
                                                 ctypes.c_float, c_size, c_vp]),
+    "nbgb_integrate_reference_ex": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_float,
+                                                   ctypes.c_float, c_size, ctypes.c_int, c_vp]),
     "nbgb_system_create": (c_vp, [c_size, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float]),
     "nbgb_system_destroy": (None, [c_vp]),
@@ -53,6 +55,7 @@ SIGNATURES = {
     "nbgb_system_synchronize": (ctypes.c_int, [c_vp]),
     "nbgb_system_set_timing": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "nbgb_system_last_force_ms": (ctypes.c_int, [c_vp, c_f32p]),
+    "nbgb_system_last_integrate_ms": (ctypes.c_int, [c_vp, c_f32p, c_f32p]),
     "nbgb_system_get_state": (ctypes.c_int, [c_vp, c_f32p, c_f32p]),
     "nbgb_system_get_state64": (ctypes.c_int, [c_vp, c_f64p, c_f64p]),
     "nbgb_system_get_force": (ctypes.c_int, [c_vp, c_f32p]),

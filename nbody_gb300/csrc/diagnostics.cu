@@ -20,10 +20,11 @@ namespace nbgb {
 constexpr int kDiagThreads = 256;
 constexpr int kDiagQ = 8;  // KE, PE, Px, Py, Pz, Lx, Ly, Lz
 
-// Source of positions / velocities / masses: FP64 SoA (KDK) when x64 != null,
-// else the FP32 float4 arrays (reference integrator).
+// Source of positions / velocities / masses: FP64 SoA (KDK; components ld
+// doubles apart) when x64 != null, else the FP32 float4 arrays (reference
+// integrator).
 __global__ void __launch_bounds__(kDiagThreads) diag_partials_kernel(
-    int n, const double *__restrict__ x64, const float *__restrict__ mass,
+    int n, const double *__restrict__ x64, size_t ld, const float *__restrict__ mass,
     const float4 *__restrict__ pm, const float4 *__restrict__ vel,
     const float4 *__restrict__ phi, double *__restrict__ part) {
     __shared__ double red[kDiagQ][kDiagThreads];
@@ -33,11 +34,11 @@ __global__ void __launch_bounds__(kDiagThreads) diag_partials_kernel(
         if (x64) {
             m = mass[i];
             x = x64[i];
-            y = x64[(size_t)n + i];
-            z = x64[2 * (size_t)n + i];
-            u = x64[3 * (size_t)n + i];
-            v = x64[4 * (size_t)n + i];
-            w = x64[5 * (size_t)n + i];
+            y = x64[ld + i];
+            z = x64[2 * ld + i];
+            u = x64[3 * ld + i];
+            v = x64[4 * ld + i];
+            w = x64[5 * ld + i];
         } else {
             const float4 p = pm[i], q = vel[i];
             m = p.w;
@@ -87,11 +88,11 @@ size_t diag_scratch_bytes() { return (size_t)(diag_blocks() + 1) * kDiagQ * size
 
 // scratch: diag_scratch_bytes() of device memory; out8 (device) receives the
 // eight sums.
-int launch_diagnostics(int n, const double *x64, const float *mass, const float4 *pm,
+int launch_diagnostics(int n, const double *x64, size_t ld, const float *mass, const float4 *pm,
                        const float4 *vel, const float4 *phi, double *scratch, double *out8,
                        cudaStream_t st) {
     const int nb = diag_blocks();
-    diag_partials_kernel<<<nb, kDiagThreads, 0, st>>>(n, x64, mass, pm, vel, phi, scratch);
+    diag_partials_kernel<<<nb, kDiagThreads, 0, st>>>(n, x64, ld, mass, pm, vel, phi, scratch);
     diag_final_kernel<<<1, 32, 0, st>>>(nb, scratch, out8);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }

@@ -552,10 +552,15 @@ constexpr int kMaxConfigs = 64;
 static_assert(sizeof(kConfigs) / sizeof(kConfigs[0]) <= (size_t)kMaxConfigs,
               "DeviceInfo::occ must hold every configuration");
 
+// Per device: SM count and resident CTAs per SM of every configuration.
+// Filling it also sets the kernels' dynamic shared-memory attributes, which
+// belong to the context, so the entry is refilled when the context changes
+// (cudaDeviceReset).
 struct DeviceInfo {
     int sms = 0;
     int occ[kMaxConfigs] = {0};
     bool ok = false;
+    unsigned long long ctx = 0;
 };
 
 static std::mutex g_dev_mu;
@@ -563,12 +568,15 @@ static DeviceInfo g_dev[64];
 
 static const DeviceInfo *device_info() {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    unsigned long long ctx = 0;
+    if (current_context(&dev, &ctx) != NBGB_OK || dev < 0 || dev >= 64)
         return nullptr;
     std::lock_guard<std::mutex> lk(g_dev_mu);
     DeviceInfo &d = g_dev[dev];
-    if (d.ok)
+    if (d.ok && d.ctx == ctx)
         return &d;
+    d.ok = false;
+    d.ctx = ctx;
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
         return nullptr;
@@ -799,19 +807,28 @@ int read_and_clear_status(unsigned *bits) {
 }
 
 // Workspace cache for the drop-in entry point (one per device, grow-only).
+// The pointer belongs to the context it was allocated in: after a
+// cudaDeviceReset (a new context id) it is dropped without being freed --
+// the reset already released it.
 struct WsCache {
     void *ptr = nullptr;
     size_t bytes = 0;
+    unsigned long long ctx = 0;
 };
 static std::mutex g_ws_mu;
 static WsCache g_ws[64];
 
 static void *cached_workspace(size_t bytes) {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    unsigned long long ctx = 0;
+    if (current_context(&dev, &ctx) != NBGB_OK || dev < 0 || dev >= 64)
         return nullptr;
     std::lock_guard<std::mutex> lk(g_ws_mu);
     WsCache &w = g_ws[dev];
+    if (w.ptr && w.ctx != ctx) {
+        w.ptr = nullptr;
+        w.bytes = 0;
+    }
     if (w.bytes >= bytes && w.ptr)
         return w.ptr;
     if (w.ptr) {
@@ -819,6 +836,7 @@ static void *cached_workspace(size_t bytes) {
         w.ptr = nullptr;
         w.bytes = 0;
     }
+    w.ctx = ctx;
     if (cudaMalloc(&w.ptr, bytes) != cudaSuccess) {
         w.ptr = nullptr;
         return nullptr;
@@ -833,8 +851,12 @@ void release_workspaces() {
     cudaGetDevice(&cur);
     for (int d = 0; d < 64; d++) {
         if (g_ws[d].ptr) {
-            cudaSetDevice(d);
-            cudaFree(g_ws[d].ptr);
+            int dev = -1;
+            unsigned long long ctx = 0;
+            // free only what the device's current context still owns
+            if (cudaSetDevice(d) == cudaSuccess && current_context(&dev, &ctx) == NBGB_OK &&
+                dev == d && ctx == g_ws[d].ctx)
+                cudaFree(g_ws[d].ptr);
             g_ws[d].ptr = nullptr;
             g_ws[d].bytes = 0;
         }

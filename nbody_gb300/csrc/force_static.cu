@@ -22,8 +22,10 @@
 //    the call's own first kernel, so calls in sequence are independent, but
 //    calls that overlap on the GPU (different streams, or host threads) race;
 //  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress, once per device, with that device current); make
-//    that first call before capturing any stream.
+//    (cudaGetSymbolAddress, once per device and context, with that device
+//    current); make that first call before capturing any stream.  After a
+//    cudaDeviceReset the next call looks the address up again in the new
+//    context.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -45,18 +47,24 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBy
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void *g_scratch_addr[kMaxDevices] = {nullptr};
+unsigned long long g_scratch_ctx[kMaxDevices] = {0};
 
-// Device address of g_static_scratch on the current device (looked up once).
+// Device address of g_static_scratch on the current device, looked up once
+// per device and context (a reset context loads the module again, possibly
+// at another address).
 int scratch_address(void **out) {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    unsigned long long ctx = 0;
+    if (current_context(&dev, &ctx) != NBGB_OK || dev < 0 || dev >= kMaxDevices)
         return NBGB_ERR_CUDA;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_addr[dev]) {
+    if (!g_scratch_addr[dev] || g_scratch_ctx[dev] != ctx) {
         void *p = nullptr;
+        g_scratch_addr[dev] = nullptr;
         if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p)
             return NBGB_ERR_CUDA;
         g_scratch_addr[dev] = p;
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_addr[dev];
     return NBGB_OK;

@@ -6,17 +6,29 @@
 //     v += (F * invMass) * dt;  v *= damping;  x += v * dt
 // in binary32 with every product and sum rounded separately (no FMA
 // contraction), which is bit-identical to the same formula evaluated in IEEE
-// single precision on the host.  The reference runs this on one host thread
-// after copying forces back; here it is an HBM-bound kernel (80 B/body:
-// read posMass, velInvMass, force; write posMass, velInvMass) that can also
-// write the paired j-stream for the next force pass, so a resident step is
-// force -> integrate with no host round trip.
+// single precision on the host.  The fused-drift variant computes
+// x = fma(v, dt, x) instead: that is what the reference binary itself
+// computes when built with its own flags (meson.build:33-38, -O3 -ffast-math
+// -march=native: GCC contracts the position update and leaves the velocity
+// update as written), bit for bit.  The reference runs this on one host
+// thread after copying forces back; here it is an HBM-bound kernel (80 B per
+// body: read posMass, velInvMass, force; write posMass, velInvMass) that can
+// also write the paired j-stream for the next force pass (+16 B), so a
+// resident step is force -> integrate with no host round trip.
 //
 // Physics mode (no reference counterpart) is FP64 kick-drift-kick leapfrog:
-// positions and velocities live in FP64 (SoA), the force kernel's output is
-// the acceleration (a = F: the sum already carries m_j), no damping.  The
-// kick/drift kernel writes the FP32 posMass {x,y,z,m} and j-stream the next
-// FP32 force pass reads.
+// positions and velocities live in FP64 (SoA, leading dimension ld, even),
+// the force kernel's output is the acceleration (a = F: the sum already
+// carries m_j), no damping.  Two kernels:
+//   kick_drift  v += a * kick; x += v * dt; writes x, v, the FP32 posMass
+//               {x,y,z,m} and the j-stream the next force pass reads
+//               (148 B per body: read x, v 48, a 16, m 4; write x, v 48,
+//               posMass 16, j-stream 16)
+//   half_kick   v += a * dt/2, closing a leapfrog step (64 B per body: read
+//               v 24, a 16; write v 24)
+// Each thread owns one body pair (2q, 2q+1): FP64 components move as one
+// 16-byte double2, FP32 masses as one float2, so every access is a 128-bit
+// (or 64-bit) coalesced vector access.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,7 +40,8 @@
 
 namespace nbgb {
 
-// Thread q owns bodies 2q and 2q+1 (one j-stream pair).
+constexpr int kIntegrateThreads = 256;
+
 // j-stream store for bodies 2q, 2q+1 in either layout (vpb 1: source pairs,
 // vpb 2: each source duplicated); logm: log2 masses in the pairs that carry
 // them in log-domain plans.
@@ -49,32 +62,51 @@ __device__ __forceinline__ void store_jstream(float4 *__restrict__ js, int vpb, 
     }
 }
 
-__global__ void integrate_reference_kernel(float4 *__restrict__ pm, float4 *__restrict__ vel,
-                                           const float4 *__restrict__ force, float dt,
-                                           float damping, int n, float4 *__restrict__ js,
-                                           int js_vpb, int js_log, int npad,
-                                           unsigned *__restrict__ counters, int ncounters) {
+template <bool FUSED_DRIFT>
+__device__ __forceinline__ float drift(float x, float v, float dt) {
+    if constexpr (FUSED_DRIFT)
+        return __fmaf_rn(v, dt, x);
+    else
+        return __fadd_rn(x, __fmul_rn(v, dt));
+}
+
+// Thread q owns bodies 2q and 2q+1 (one j-stream pair).
+template <bool FUSED_DRIFT>
+__global__ void __launch_bounds__(kIntegrateThreads)
+    integrate_reference_kernel(float4 *__restrict__ pm, float4 *__restrict__ vel,
+                               const float4 *__restrict__ force, float dt, float damping, int n,
+                               float4 *__restrict__ js, int js_vpb, int js_log, int npad,
+                               unsigned *__restrict__ counters, int ncounters) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < ncounters)
         counters[q] = 0u;
     float4 out[2];
+    float4 p[2], v[2], f[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {  // all loads first (memory-level parallelism)
+        const int i = 2 * q + h;
+        if (i < n) {
+            p[h] = pm[i];
+            v[h] = vel[i];
+            f[h] = force[i];
+        }
+    }
 #pragma unroll
     for (int h = 0; h < 2; h++) {
         const int i = 2 * q + h;
         if (i < n) {
-            float4 p = pm[i];
-            float4 v = vel[i];
-            const float4 f = force[i];
-            const float im = v.w;
-            v.x = __fmul_rn(__fadd_rn(v.x, __fmul_rn(__fmul_rn(f.x, im), dt)), damping);
-            v.y = __fmul_rn(__fadd_rn(v.y, __fmul_rn(__fmul_rn(f.y, im), dt)), damping);
-            v.z = __fmul_rn(__fadd_rn(v.z, __fmul_rn(__fmul_rn(f.z, im), dt)), damping);
-            p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
-            p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
-            p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
-            pm[i] = p;
-            vel[i] = v;
-            out[h] = p;
+            float4 pp = p[h], vv = v[h];
+            const float4 ff = f[h];
+            const float im = vv.w;
+            vv.x = __fmul_rn(__fadd_rn(vv.x, __fmul_rn(__fmul_rn(ff.x, im), dt)), damping);
+            vv.y = __fmul_rn(__fadd_rn(vv.y, __fmul_rn(__fmul_rn(ff.y, im), dt)), damping);
+            vv.z = __fmul_rn(__fadd_rn(vv.z, __fmul_rn(__fmul_rn(ff.z, im), dt)), damping);
+            pp.x = drift<FUSED_DRIFT>(pp.x, vv.x, dt);
+            pp.y = drift<FUSED_DRIFT>(pp.y, vv.y, dt);
+            pp.z = drift<FUSED_DRIFT>(pp.z, vv.z, dt);
+            pm[i] = pp;
+            vel[i] = vv;
+            out[h] = pp;
         } else {
             out[h] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
@@ -83,74 +115,135 @@ __global__ void integrate_reference_kernel(float4 *__restrict__ pm, float4 *__re
         store_jstream(js, js_vpb, js_log, q, out[0], out[1]);
 }
 
-// FP64 kick (v += a * kick_dt) then drift (x += v * drift_dt); either may be
-// 0.  Writes posMass (FP32) and, if js != nullptr, the paired j-stream.
-__global__ void kdk_kernel(double *__restrict__ px, double *__restrict__ py,
-                           double *__restrict__ pz, double *__restrict__ vx,
-                           double *__restrict__ vy, double *__restrict__ vz,
-                           const float *__restrict__ mass, const float4 *__restrict__ accel,
-                           double kick_dt, double drift_dt, int write_pos, int n,
-                           float4 *__restrict__ pm, float4 *__restrict__ js, int js_vpb,
-                           int js_log, int npad, unsigned *__restrict__ counters, int ncounters) {
+__device__ __forceinline__ double2 ld_d2(const double *p) {
+    return *reinterpret_cast<const double2 *>(p);
+}
+__device__ __forceinline__ void st_d2(double *p, double a, double b) {
+    *reinterpret_cast<double2 *>(p) = make_double2(a, b);
+}
+
+// FP64 kick then drift of bodies 2q, 2q+1: v += a * kick_dt (skipped when
+// kick_dt == 0), x += v * drift_dt; writes x, v, posMass and (js != null)
+// the j-stream pair q.  x64: six SoA components of leading dimension ld
+// (even; entries n..ld-1 are padding).
+__global__ void __launch_bounds__(kIntegrateThreads)
+    kick_drift_kernel(double *__restrict__ x64, size_t ld, const float *__restrict__ mass,
+                      const float4 *__restrict__ accel, double kick_dt, double drift_dt, int n,
+                      float4 *__restrict__ pm, float4 *__restrict__ js, int js_vpb, int js_log,
+                      int npad, unsigned *__restrict__ counters, int ncounters) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < ncounters)
         counters[q] = 0u;
-    float4 out[2];
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int i = 2 * q + h;
-        if (i < n) {
-            double x = px[i], y = py[i], z = pz[i];
-            double u = vx[i], v = vy[i], w = vz[i];
-            if (kick_dt != 0.0) {
-                const float4 a = accel[i];
-                u = fma((double)a.x, kick_dt, u);
-                v = fma((double)a.y, kick_dt, v);
-                w = fma((double)a.z, kick_dt, w);
-                vx[i] = u;
-                vy[i] = v;
-                vz[i] = w;
-            }
-            if (drift_dt != 0.0) {
-                x = fma(u, drift_dt, x);
-                y = fma(v, drift_dt, y);
-                z = fma(w, drift_dt, z);
-                px[i] = x;
-                py[i] = y;
-                pz[i] = z;
-            }
-            out[h] = make_float4((float)x, (float)y, (float)z, mass[i]);
-            if (write_pos)
-                pm[i] = out[h];
-        } else {
-            out[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int i0 = 2 * q;
+    float4 out0 = make_float4(0.f, 0.f, 0.f, 0.f), out1 = out0;
+    if (i0 < n) {
+        const bool two = i0 + 1 < n;
+        double2 X = ld_d2(x64 + i0), Y = ld_d2(x64 + ld + i0), Z = ld_d2(x64 + 2 * ld + i0);
+        double2 U = ld_d2(x64 + 3 * ld + i0), V = ld_d2(x64 + 4 * ld + i0),
+                W = ld_d2(x64 + 5 * ld + i0);
+        const float4 a0 = accel[i0];
+        const float4 a1 = two ? accel[i0 + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 m;
+        if (two)
+            m = *reinterpret_cast<const float2 *>(mass + i0);
+        else
+            m = make_float2(mass[i0], 0.f);
+        if (kick_dt != 0.0) {
+            U.x = fma((double)a0.x, kick_dt, U.x);
+            V.x = fma((double)a0.y, kick_dt, V.x);
+            W.x = fma((double)a0.z, kick_dt, W.x);
+            U.y = fma((double)a1.x, kick_dt, U.y);
+            V.y = fma((double)a1.y, kick_dt, V.y);
+            W.y = fma((double)a1.z, kick_dt, W.y);
+        }
+        X.x = fma(U.x, drift_dt, X.x);
+        Y.x = fma(V.x, drift_dt, Y.x);
+        Z.x = fma(W.x, drift_dt, Z.x);
+        X.y = fma(U.y, drift_dt, X.y);
+        Y.y = fma(V.y, drift_dt, Y.y);
+        Z.y = fma(W.y, drift_dt, Z.y);
+        // the padding entry of an odd n is written back as read
+        st_d2(x64 + i0, X.x, X.y);
+        st_d2(x64 + ld + i0, Y.x, Y.y);
+        st_d2(x64 + 2 * ld + i0, Z.x, Z.y);
+        st_d2(x64 + 3 * ld + i0, U.x, U.y);
+        st_d2(x64 + 4 * ld + i0, V.x, V.y);
+        st_d2(x64 + 5 * ld + i0, W.x, W.y);
+        out0 = make_float4((float)X.x, (float)Y.x, (float)Z.x, m.x);
+        pm[i0] = out0;
+        if (two) {
+            out1 = make_float4((float)X.y, (float)Y.y, (float)Z.y, m.y);
+            pm[i0 + 1] = out1;
         }
     }
-    if (write_pos && js && 2 * q < npad)
-        store_jstream(js, js_vpb, js_log, q, out[0], out[1]);
+    if (js && i0 < npad)
+        store_jstream(js, js_vpb, js_log, q, out0, out1);
+}
+
+// FP64 kick of bodies 2q, 2q+1: v += a * kick_dt.
+__global__ void __launch_bounds__(kIntegrateThreads)
+    half_kick_kernel(double *__restrict__ x64, size_t ld, const float4 *__restrict__ accel,
+                     double kick_dt, int n) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i0 = 2 * q;
+    if (i0 >= n)
+        return;
+    const bool two = i0 + 1 < n;
+    double *u = x64 + 3 * ld + i0, *v = x64 + 4 * ld + i0, *w = x64 + 5 * ld + i0;
+    double2 U = ld_d2(u), V = ld_d2(v), W = ld_d2(w);
+    const float4 a0 = accel[i0];
+    const float4 a1 = two ? accel[i0 + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+    U.x = fma((double)a0.x, kick_dt, U.x);
+    V.x = fma((double)a0.y, kick_dt, V.x);
+    W.x = fma((double)a0.z, kick_dt, W.x);
+    U.y = fma((double)a1.x, kick_dt, U.y);
+    V.y = fma((double)a1.y, kick_dt, V.y);
+    W.y = fma((double)a1.z, kick_dt, W.y);
+    st_d2(u, U.x, U.y);
+    st_d2(v, V.x, V.y);
+    st_d2(w, W.x, W.y);
+}
+
+static inline unsigned blocks_for(int work) {
+    return (unsigned)((std::max(work, 1) + kIntegrateThreads - 1) / kIntegrateThreads);
 }
 
 int launch_integrate_reference(float4 *pm, float4 *vel, const float4 *force, float dt,
-                               float damping, size_t n, float4 *js, int js_vpb, int js_log,
-                               int npad, unsigned *counters, int ncounters, cudaStream_t st) {
+                               float damping, size_t n, int fused_drift, float4 *js, int js_vpb,
+                               int js_log, int npad, unsigned *counters, int ncounters,
+                               cudaStream_t st) {
     const int pairs = (int)((n + 1) / 2);
     const int work = std::max(std::max(pairs, npad / 2), ncounters);
-    const int tb = 256;
-    integrate_reference_kernel<<<(work + tb - 1) / tb, tb, 0, st>>>(
-        pm, vel, force, dt, damping, (int)n, js, js_vpb, js_log, npad, counters, ncounters);
+    if (fused_drift)
+        integrate_reference_kernel<true><<<blocks_for(work), kIntegrateThreads, 0, st>>>(
+            pm, vel, force, dt, damping, (int)n, js, js_vpb, js_log, npad, counters, ncounters);
+    else
+        integrate_reference_kernel<false><<<blocks_for(work), kIntegrateThreads, 0, st>>>(
+            pm, vel, force, dt, damping, (int)n, js, js_vpb, js_log, npad, counters, ncounters);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
-int launch_kdk(double *px, double *py, double *pz, double *vx, double *vy, double *vz,
-               const float *mass, const float4 *accel, double kick_dt, double drift_dt,
-               int write_pos, size_t n, float4 *pm, float4 *js, int js_vpb, int js_log, int npad,
-               unsigned *counters, int ncounters, cudaStream_t st) {
+int launch_kick_drift(double *x64, size_t ld, const float *mass, const float4 *accel,
+                      double kick_dt, double drift_dt, size_t n, float4 *pm, float4 *js,
+                      int js_vpb, int js_log, int npad, unsigned *counters, int ncounters,
+                      cudaStream_t st) {
+    if ((ld & 1) || ld < n)
+        return NBGB_ERR_INVALID_ARGUMENT;
     const int pairs = (int)((n + 1) / 2);
     const int work = std::max(std::max(pairs, npad / 2), ncounters);
-    const int tb = 256;
-    kdk_kernel<<<(work + tb - 1) / tb, tb, 0, st>>>(px, py, pz, vx, vy, vz, mass, accel, kick_dt,
-                                                    drift_dt, write_pos, (int)n, pm, js, js_vpb,
-                                                    js_log, npad, counters, ncounters);
+    kick_drift_kernel<<<blocks_for(work), kIntegrateThreads, 0, st>>>(
+        x64, ld, mass, accel, kick_dt, drift_dt, (int)n, pm, js, js_vpb, js_log, npad, counters,
+        ncounters);
+    return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
+}
+
+int launch_half_kick(double *x64, size_t ld, const float4 *accel, double kick_dt, size_t n,
+                     cudaStream_t st) {
+    if ((ld & 1) || ld < n)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const int pairs = (int)((n + 1) / 2);
+    half_kick_kernel<<<blocks_for(pairs), kIntegrateThreads, 0, st>>>(x64, ld, accel, kick_dt,
+                                                                      (int)n);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
@@ -162,17 +255,24 @@ int read_status_integrate(unsigned *bits) { return read_status_integrate_tu(bits
 
 extern "C" {
 
-NBGB_API int nbgb_integrate_reference(float *posMass, float *velInvMass, const float *force,
-                                      float dt, float damping, size_t N, void *stream) {
+NBGB_API int nbgb_integrate_reference_ex(float *posMass, float *velInvMass, const float *force,
+                                         float dt, float damping, size_t N, int fused_drift,
+                                         void *stream) {
     if (N == 0)
         return NBGB_OK;
-    if (!posMass || !velInvMass || !force || N > nbgb::kMaxBodies)
+    if (!posMass || !velInvMass || !force || N > nbgb::kMaxBodies ||
+        (fused_drift != 0 && fused_drift != 1))
         return NBGB_ERR_INVALID_ARGUMENT;
     if (((uintptr_t)posMass | (uintptr_t)velInvMass | (uintptr_t)force) & 15u)
         return NBGB_ERR_INVALID_ARGUMENT;
     return nbgb::launch_integrate_reference((float4 *)posMass, (float4 *)velInvMass,
-                                            (const float4 *)force, dt, damping, N, nullptr, 1, 0,
-                                            0, nullptr, 0, (cudaStream_t)stream);
+                                            (const float4 *)force, dt, damping, N, fused_drift,
+                                            nullptr, 1, 0, 0, nullptr, 0, (cudaStream_t)stream);
+}
+
+NBGB_API int nbgb_integrate_reference(float *posMass, float *velInvMass, const float *force,
+                                      float dt, float damping, size_t N, void *stream) {
+    return nbgb_integrate_reference_ex(posMass, velInvMass, force, dt, damping, N, 0, stream);
 }
 
 }  // extern "C"

@@ -11,6 +11,12 @@ namespace nbgb {
 // Largest N any entry point accepts (indices are 32-bit inside the kernels).
 constexpr size_t kMaxBodies = (size_t)1 << 30;
 
+// The current device and the id of the CUDA context current on this thread
+// (unique within the process; a context re-created after cudaDeviceReset has
+// a new id).  Per-device caches compare it to detect a reset.  NBGB_OK or
+// NBGB_ERR_CUDA.
+int current_context(int *device, unsigned long long *ctx_id);
+
 // One force evaluation's decomposition and workspace layout.
 struct ForcePlan {
     int config = 0;       // index into the kernel configuration table
@@ -40,15 +46,21 @@ int read_and_clear_status(unsigned *bits);
 int read_status_ensemble(unsigned *bits);
 int read_status_integrate(unsigned *bits);
 // js_vpb, js_log: j-stream layout of the plan the j-stream is written for.
+// fused_drift: x = fma(v, dt, x), as the reference's own build computes it.
 int launch_integrate_reference(float4 *pm, float4 *vel, const float4 *force, float dt,
-                               float damping, size_t n, float4 *js, int js_vpb, int js_log,
-                               int npad, unsigned *counters, int ncounters, cudaStream_t st);
-int launch_kdk(double *px, double *py, double *pz, double *vx, double *vy, double *vz,
-               const float *mass, const float4 *accel, double kick_dt, double drift_dt,
-               int write_pos, size_t n, float4 *pm, float4 *js, int js_vpb, int js_log, int npad,
-               unsigned *counters, int ncounters, cudaStream_t st);
+                               float damping, size_t n, int fused_drift, float4 *js, int js_vpb,
+                               int js_log, int npad, unsigned *counters, int ncounters,
+                               cudaStream_t st);
+// FP64 SoA state x64 = [x, y, z, vx, vy, vz], each component ld doubles
+// (ld even, >= n).
+int launch_kick_drift(double *x64, size_t ld, const float *mass, const float4 *accel,
+                      double kick_dt, double drift_dt, size_t n, float4 *pm, float4 *js,
+                      int js_vpb, int js_log, int npad, unsigned *counters, int ncounters,
+                      cudaStream_t st);
+int launch_half_kick(double *x64, size_t ld, const float4 *accel, double kick_dt, size_t n,
+                     cudaStream_t st);
 size_t diag_scratch_bytes();
-int launch_diagnostics(int n, const double *x64, const float *mass, const float4 *pm,
+int launch_diagnostics(int n, const double *x64, size_t ld, const float *mass, const float4 *pm,
                        const float4 *vel, const float4 *phi, double *scratch, double *out8,
                        cudaStream_t st);
 // Newton-3 evaluation of many systems in one launch (the ensemble): one

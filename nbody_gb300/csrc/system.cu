@@ -8,10 +8,17 @@
 // force launch plus one integrate launch that also writes the next step's
 // j-stream, captured once into a CUDA graph and replayed.
 //
-// Two integrators:
-//   NBGB_INTEGRATOR_REFERENCE  integrateOne (src/nbody.cu:158-182), FP32,
-//                              damping, invMass from velInvMass.w
-//   NBGB_INTEGRATOR_KDK64      FP64 kick-drift-kick leapfrog, a = F, no damping
+// Integrators:
+//   NBGB_INTEGRATOR_REFERENCE        integrateOne (src/nbody.cu:158-182),
+//                                    FP32, damping, invMass from
+//                                    velInvMass.w, each operation rounded
+//   NBGB_INTEGRATOR_REFERENCE_FUSED  the same with x = fma(v, dt, x), as the
+//                                    reference binary computes it
+//   NBGB_INTEGRATOR_KDK64            FP64 kick-drift-kick leapfrog, a = F,
+//                                    no damping
+//
+// Timing mode brackets every force launch and every integrate launch with
+// CUDA events on the system's stream (the step then runs eagerly).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -36,7 +43,8 @@ struct nbgb_system {
     float4 *pm = nullptr;     // posMass {x,y,z,m} (FP32, what the force pass reads)
     float4 *vel = nullptr;    // velInvMass {vx,vy,vz,1/m} (reference integrator)
     float4 *force = nullptr;  // force / acceleration {fx,fy,fz,0}
-    double *x64 = nullptr;    // KDK: px,py,pz,vx,vy,vz (6 * n doubles)
+    double *x64 = nullptr;    // KDK: px,py,pz,vx,vy,vz (6 components, ld apart)
+    size_t ld = 0;            // KDK: leading dimension of x64 (n rounded up to 64)
     float *mass = nullptr;    // KDK: m
     void *ws = nullptr;
     size_t ws_bytes = 0;
@@ -48,6 +56,10 @@ struct nbgb_system {
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed_once = false;
+    // integrate launches: [0,1] reference integrate or kick+drift, [2,3] the
+    // closing half kick (KDK)
+    cudaEvent_t iev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool itimed = false, htimed = false;
     // force algorithm: 0 one-sided (planned kernel), 1 Newton's third law
     int algorithm = 0;
     void *ws_n3 = nullptr;
@@ -70,7 +82,18 @@ unsigned *cnt_of(nbgb_system *s) {
 int ncnt_of(nbgb_system *s) { return s->plan.nsplit > 1 ? s->plan.nblocks : 0; }
 int npad_of(nbgb_system *s) { return s->plan.ntiles * s->plan.tile_bodies; }
 
-double *comp(nbgb_system *s, int c) { return s->x64 + (size_t)c * s->n; }
+double *comp(nbgb_system *s, int c) { return s->x64 + (size_t)c * s->ld; }
+
+bool reference_integrator(int integrator) {
+    return integrator == NBGB_INTEGRATOR_REFERENCE || integrator == NBGB_INTEGRATOR_REFERENCE_FUSED;
+}
+
+// Event pair k (0: integrate / kick+drift, 1: half kick) around a launch.
+int mark(nbgb_system *s, int ev) {
+    if (s->timing && cudaEventRecord(s->iev[ev], s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    return NBGB_OK;
+}
 
 int ensure_jstream(nbgb_system *s) {
     if (s->js_valid)
@@ -111,28 +134,39 @@ int timed_force(nbgb_system *s) {
 // One reference step: force(x) then integrate (writes x' and its j-stream).
 int ref_step_body(nbgb_system *s) {
     int rc = timed_force(s);
-    if (rc != NBGB_OK)
-        return rc;
-    return nbgb::launch_integrate_reference(s->pm, s->vel, s->force, s->dt, s->damping, s->n,
-                                            js_of(s), s->plan.js_vpb, s->plan.js_log, npad_of(s),
-                                            cnt_of(s), ncnt_of(s), s->stream);
+    if (rc == NBGB_OK)
+        rc = mark(s, 0);
+    if (rc == NBGB_OK)
+        rc = nbgb::launch_integrate_reference(
+            s->pm, s->vel, s->force, s->dt, s->damping, s->n,
+            s->integrator == NBGB_INTEGRATOR_REFERENCE_FUSED ? 1 : 0, js_of(s), s->plan.js_vpb,
+            s->plan.js_log, npad_of(s), cnt_of(s), ncnt_of(s), s->stream);
+    if (rc == NBGB_OK && (rc = mark(s, 1)) == NBGB_OK && s->timing)
+        s->itimed = true;
+    return rc;
 }
 
 // One fused leapfrog body: v += a*kick; x += v*dt; a = F(x).
 int kdk_body(nbgb_system *s, double kick) {
-    int rc = nbgb::launch_kdk(comp(s, 0), comp(s, 1), comp(s, 2), comp(s, 3), comp(s, 4),
-                              comp(s, 5), s->mass, s->force, kick, (double)s->dt, 1, s->n, s->pm,
-                              js_of(s), s->plan.js_vpb, s->plan.js_log, npad_of(s), cnt_of(s),
-                              ncnt_of(s), s->stream);
+    int rc = mark(s, 0);
+    if (rc == NBGB_OK)
+        rc = nbgb::launch_kick_drift(s->x64, s->ld, s->mass, s->force, kick, (double)s->dt, s->n,
+                                     s->pm, js_of(s), s->plan.js_vpb, s->plan.js_log, npad_of(s),
+                                     cnt_of(s), ncnt_of(s), s->stream);
+    if (rc == NBGB_OK && (rc = mark(s, 1)) == NBGB_OK && s->timing)
+        s->itimed = true;
     if (rc != NBGB_OK)
         return rc;
     return timed_force(s);
 }
 
 int half_kick(nbgb_system *s) {
-    return nbgb::launch_kdk(comp(s, 0), comp(s, 1), comp(s, 2), comp(s, 3), comp(s, 4), comp(s, 5),
-                            s->mass, s->force, 0.5 * (double)s->dt, 0.0, 0, s->n, s->pm, nullptr, 1,
-                            0, 0, nullptr, 0, s->stream);
+    int rc = mark(s, 2);
+    if (rc == NBGB_OK)
+        rc = nbgb::launch_half_kick(s->x64, s->ld, s->force, 0.5 * (double)s->dt, s->n, s->stream);
+    if (rc == NBGB_OK && (rc = mark(s, 3)) == NBGB_OK && s->timing)
+        s->htimed = true;
+    return rc;
 }
 
 // Masses below zero (or NaN) have no logarithm: a system whose plan takes
@@ -186,6 +220,9 @@ void free_all(nbgb_system *s) {
         cudaEventDestroy(s->ev0);
     if (s->ev1)
         cudaEventDestroy(s->ev1);
+    for (cudaEvent_t e : s->iev)
+        if (e)
+            cudaEventDestroy(e);
     cudaFree(s->pm);
     cudaFree(s->vel);
     cudaFree(s->force);
@@ -209,8 +246,7 @@ int build_graph(nbgb_system *s) {
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return NBGB_ERR_CUDA;
-    int rc = (s->integrator == NBGB_INTEGRATOR_REFERENCE) ? ref_step_body(s)
-                                                          : kdk_body(s, (double)s->dt);
+    int rc = reference_integrator(s->integrator) ? ref_step_body(s) : kdk_body(s, (double)s->dt);
     cudaError_t e = cudaStreamEndCapture(s->stream, &g);
     if (rc != NBGB_OK || e != cudaSuccess) {
         if (g)
@@ -230,7 +266,7 @@ NBGB_API nbgb_system *nbgb_system_create(size_t N, int integrator, float softeni
                                          float damping) {
     if (N == 0 || N > nbgb::kMaxBodies)
         return nullptr;
-    if (integrator != NBGB_INTEGRATOR_REFERENCE && integrator != NBGB_INTEGRATOR_KDK64)
+    if (!reference_integrator(integrator) && integrator != NBGB_INTEGRATOR_KDK64)
         return nullptr;
     nbgb_system *s = new (std::nothrow) nbgb_system();
     if (!s)
@@ -247,10 +283,13 @@ NBGB_API nbgb_system *nbgb_system_create(size_t N, int integrator, float softeni
     ok = ok && cudaMalloc(&s->force, N * 16) == cudaSuccess;
     ok = ok && cudaMalloc(&s->ws, s->plan.workspace_bytes) == cudaSuccess;
     s->ws_bytes = s->plan.workspace_bytes;
-    if (integrator == NBGB_INTEGRATOR_REFERENCE) {
+    if (reference_integrator(integrator)) {
         ok = ok && cudaMalloc(&s->vel, N * 16) == cudaSuccess;
     } else {
-        ok = ok && cudaMalloc(&s->x64, N * 6 * sizeof(double)) == cudaSuccess;
+        s->ld = (N + 63) / 64 * 64;
+        ok = ok && cudaMalloc(&s->x64, s->ld * 6 * sizeof(double)) == cudaSuccess;
+        // padding entries stay zero (the pair kernels read and rewrite them)
+        ok = ok && cudaMemsetAsync(s->x64, 0, s->ld * 6 * sizeof(double), s->stream) == cudaSuccess;
         ok = ok && cudaMalloc(&s->mass, N * sizeof(float)) == cudaSuccess;
     }
     ok = ok && cudaMemsetAsync(s->force, 0, N * 16, s->stream) == cudaSuccess;
@@ -292,21 +331,22 @@ NBGB_API int nbgb_system_set_state(nbgb_system *s, const float *posMass, const f
         return rc;
     if (cudaMemcpyAsync(s->pm, posMass, n * 16, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
         return NBGB_ERR_CUDA;
-    if (s->integrator == NBGB_INTEGRATOR_REFERENCE) {
+    if (reference_integrator(s->integrator)) {
         if (cudaMemcpyAsync(s->vel, velInvMass, n * 16, cudaMemcpyHostToDevice, s->stream) !=
             cudaSuccess)
             return NBGB_ERR_CUDA;
     } else {
-        std::vector<double> h(n * 6);
+        const size_t ld = s->ld;
+        std::vector<double> h(ld * 6, 0.0);
         std::vector<float> m(n);
         for (size_t i = 0; i < n; i++) {
             for (int c = 0; c < 3; c++) {
-                h[c * n + i] = posMass[4 * i + c];
-                h[(3 + c) * n + i] = velInvMass[4 * i + c];
+                h[c * ld + i] = posMass[4 * i + c];
+                h[(3 + c) * ld + i] = velInvMass[4 * i + c];
             }
             m[i] = posMass[4 * i + 3];
         }
-        if (cudaMemcpyAsync(s->x64, h.data(), n * 6 * sizeof(double), cudaMemcpyHostToDevice,
+        if (cudaMemcpyAsync(s->x64, h.data(), ld * 6 * sizeof(double), cudaMemcpyHostToDevice,
                             s->stream) != cudaSuccess ||
             cudaMemcpyAsync(s->mass, m.data(), n * sizeof(float), cudaMemcpyHostToDevice,
                             s->stream) != cudaSuccess ||
@@ -327,17 +367,18 @@ NBGB_API int nbgb_system_set_state64(nbgb_system *s, const double *pos3, const d
     int rc = fit_plan_to_masses(s, mass, 1);
     if (rc != NBGB_OK)
         return rc;
-    std::vector<double> h(n * 6);
+    const size_t ld = s->ld;
+    std::vector<double> h(ld * 6, 0.0);
     std::vector<float> pm(n * 4);
     for (size_t i = 0; i < n; i++) {
         for (int c = 0; c < 3; c++) {
-            h[c * n + i] = pos3[3 * i + c];
-            h[(3 + c) * n + i] = vel3[3 * i + c];
+            h[c * ld + i] = pos3[3 * i + c];
+            h[(3 + c) * ld + i] = vel3[3 * i + c];
             pm[4 * i + c] = (float)pos3[3 * i + c];
         }
         pm[4 * i + 3] = mass[i];
     }
-    if (cudaMemcpyAsync(s->x64, h.data(), n * 6 * sizeof(double), cudaMemcpyHostToDevice,
+    if (cudaMemcpyAsync(s->x64, h.data(), ld * 6 * sizeof(double), cudaMemcpyHostToDevice,
                         s->stream) != cudaSuccess ||
         cudaMemcpyAsync(s->mass, mass, n * sizeof(float), cudaMemcpyHostToDevice, s->stream) !=
             cudaSuccess ||
@@ -359,7 +400,7 @@ NBGB_API int nbgb_system_step(nbgb_system *s, int nsteps) {
     if (rc != NBGB_OK)
         return rc;
     const bool graph = s->use_graph && !s->timing;
-    if (s->integrator == NBGB_INTEGRATOR_REFERENCE) {
+    if (reference_integrator(s->integrator)) {
         if (graph && (rc = build_graph(s)) != NBGB_OK)
             return rc;
         for (int k = 0; k < nsteps; k++) {
@@ -422,9 +463,31 @@ NBGB_API int nbgb_system_set_timing(nbgb_system *s, int enable) {
     if (enable && !s->ev0) {
         if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess)
             return NBGB_ERR_CUDA;
+        for (cudaEvent_t &e : s->iev)
+            if (cudaEventCreate(&e) != cudaSuccess)
+                return NBGB_ERR_CUDA;
     }
     s->timing = enable != 0;
     s->timed_once = false;
+    s->itimed = s->htimed = false;
+    return NBGB_OK;
+}
+
+// Milliseconds of the most recent timed integrate launches (waits for them):
+// step_ms the reference integrate or the FP64 kick+drift, half_kick_ms the
+// closing FP64 half kick (0 when none ran, e.g. reference integrators).
+NBGB_API int nbgb_system_last_integrate_ms(nbgb_system *s, float *step_ms, float *half_kick_ms) {
+    if (!s || !s->timing || !s->itimed)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (step_ms && (cudaEventSynchronize(s->iev[1]) != cudaSuccess ||
+                    cudaEventElapsedTime(step_ms, s->iev[0], s->iev[1]) != cudaSuccess))
+        return NBGB_ERR_CUDA;
+    if (half_kick_ms) {
+        *half_kick_ms = 0.f;
+        if (s->htimed && (cudaEventSynchronize(s->iev[3]) != cudaSuccess ||
+                          cudaEventElapsedTime(half_kick_ms, s->iev[2], s->iev[3]) != cudaSuccess))
+            return NBGB_ERR_CUDA;
+    }
     return NBGB_OK;
 }
 
@@ -454,14 +517,15 @@ NBGB_API int nbgb_system_get_state(nbgb_system *s, float *posMass, float *velInv
         cudaMemcpyAsync(posMass, s->pm, n * 16, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
         return NBGB_ERR_CUDA;
     if (velInvMass) {
-        if (s->integrator == NBGB_INTEGRATOR_REFERENCE) {
+        if (reference_integrator(s->integrator)) {
             if (cudaMemcpyAsync(velInvMass, s->vel, n * 16, cudaMemcpyDeviceToHost, s->stream) !=
                 cudaSuccess)
                 return NBGB_ERR_CUDA;
         } else {
-            std::vector<double> h(n * 3);
+            const size_t ld = s->ld;
+            std::vector<double> h(ld * 3);
             std::vector<float> m(n);
-            if (cudaMemcpyAsync(h.data(), comp(s, 3), n * 3 * sizeof(double),
+            if (cudaMemcpyAsync(h.data(), comp(s, 3), ld * 3 * sizeof(double),
                                 cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
                 cudaMemcpyAsync(m.data(), s->mass, n * sizeof(float), cudaMemcpyDeviceToHost,
                                 s->stream) != cudaSuccess ||
@@ -469,7 +533,7 @@ NBGB_API int nbgb_system_get_state(nbgb_system *s, float *posMass, float *velInv
                 return NBGB_ERR_CUDA;
             for (size_t i = 0; i < n; i++) {
                 for (int c = 0; c < 3; c++)
-                    velInvMass[4 * i + c] = (float)h[c * n + i];
+                    velInvMass[4 * i + c] = (float)h[c * ld + i];
                 velInvMass[4 * i + 3] = 1.0f / m[i];
             }
         }
@@ -482,18 +546,18 @@ NBGB_API int nbgb_system_get_state(nbgb_system *s, float *posMass, float *velInv
 NBGB_API int nbgb_system_get_state64(nbgb_system *s, double *pos3, double *vel3) {
     if (!s || s->integrator != NBGB_INTEGRATOR_KDK64)
         return NBGB_ERR_INVALID_ARGUMENT;
-    const size_t n = s->n;
-    std::vector<double> h(n * 6);
-    if (cudaMemcpyAsync(h.data(), s->x64, n * 6 * sizeof(double), cudaMemcpyDeviceToHost,
+    const size_t n = s->n, ld = s->ld;
+    std::vector<double> h(ld * 6);
+    if (cudaMemcpyAsync(h.data(), s->x64, ld * 6 * sizeof(double), cudaMemcpyDeviceToHost,
                         s->stream) != cudaSuccess ||
         cudaStreamSynchronize(s->stream) != cudaSuccess)
         return NBGB_ERR_CUDA;
     for (size_t i = 0; i < n; i++)
         for (int c = 0; c < 3; c++) {
             if (pos3)
-                pos3[3 * i + c] = h[c * n + i];
+                pos3[3 * i + c] = h[c * ld + i];
             if (vel3)
-                vel3[3 * i + c] = h[(3 + c) * n + i];
+                vel3[3 * i + c] = h[(3 + c) * ld + i];
         }
     return check_device_status();
 }
@@ -533,7 +597,7 @@ NBGB_API int nbgb_system_diagnostics(nbgb_system *s, double *out) {
         rc = nbgb::launch_force(s->diag_plan, s->phi, s->pm, nullptr, s->eps2, s->diag_ws,
                                 s->stream);
     if (rc == NBGB_OK)
-        rc = nbgb::launch_diagnostics((int)n, s->x64, s->mass, s->pm, s->vel, s->phi,
+        rc = nbgb::launch_diagnostics((int)n, s->x64, s->ld, s->mass, s->pm, s->vel, s->phi,
                                       s->diag_scratch, s->diag_out, s->stream);
     if (rc != NBGB_OK)
         return rc;

@@ -116,13 +116,16 @@ def ensemble_systems(n_systems: int, n_lo: int, n_hi: int, seed: int, mass_lo: f
 
 def batched_study(n_systems: int = 4096, n_lo: int = 64, n_hi: int = 8192, steps: int = 100,
                   dt: float = 0.01, eps2: float = 1e-4, seed: int = 4096,
-                  plain_sample: int = 4096) -> dict:
+                  plain_sample: int = 4096, plain_graphs: bool = True) -> dict:
     """Every system advanced `steps` FP64 KDK steps, once through the ensemble
     (one persistent force launch per step for all systems, CUDA-graph ticks)
     and once by looping the plain single-system path over the systems (one
-    System per system, eager launches).  The plain loop may run on a seeded
-    subsample of `plain_sample` systems; its systems/s then scales by the
-    sample's share of the interactions (stated in the result)."""
+    System per system, stepped as a user of that path would: its step body
+    captured once into a CUDA graph and replayed, the graph's capture and
+    instantiation inside the timed region; plain_graphs=False launches
+    eagerly instead).  The plain loop may run on a seeded subsample of
+    `plain_sample` systems; its systems/s then scales by the sample's share
+    of the interactions (stated in the result)."""
     import torch
 
     from . import INTEGRATOR_KDK64, Ensemble, System
@@ -154,7 +157,7 @@ def batched_study(n_systems: int = 4096, n_lo: int = 64, n_hi: int = 8192, steps
         p, v, m = systems[k]
         n = p.shape[0]
         s = System(n, INTEGRATOR_KDK64, eps2, dt, 1.0)
-        s.use_graph(False)
+        s.use_graph(plain_graphs)
         s.set_state64(p, v, m)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -176,6 +179,7 @@ def batched_study(n_systems: int = 4096, n_lo: int = 64, n_hi: int = 8192, steps
         "plain_seconds_full_estimate": plain_full_s,
         "plain_systems_per_s": n_systems / plain_full_s,
         "plain_interactions_per_s": plain_inter / plain_s,
+        "plain_mode": "CUDA graph per system" if plain_graphs else "eager launches",
         "speedup": plain_full_s / ens_s,
     }
 
@@ -230,6 +234,8 @@ def main(argv=None) -> None:
     ba.add_argument("--eps2", type=float, default=1e-4)
     ba.add_argument("--seed", type=int, default=4096)
     ba.add_argument("--plain-sample", type=int, default=4096)
+    ba.add_argument("--plain-eager", action="store_true",
+                    help="loop the plain path with eager launches instead of CUDA graphs")
     fo = sub.add_parser("forms")
     fo.add_argument("--n", type=int, default=262144)
     fo.add_argument("--sample", type=int, default=4096)
@@ -240,7 +246,7 @@ def main(argv=None) -> None:
         r = precision_study(a.n, a.steps, a.dt, a.eps2, a.seed, a.sample, a.every)
     else:
         r = batched_study(a.systems, a.n_lo, a.n_hi, a.steps, a.dt, a.eps2, a.seed,
-                          a.plain_sample)
+                          a.plain_sample, not a.plain_eager)
     print(json.dumps(r))
 
 

@@ -89,6 +89,41 @@ ORC_EXPORT void orc_forces_aos(float *force, const float *posMass, float eps2, s
     }
 }
 
+/* CPU_AOS's per-target loop (src/nbody_CPU_AOS.cpp:60-95) for a list of    */
+/* targets only: row t of force (float4) is body idx[t] against all N        */
+/* sources, summed exactly as orc_forces_aos sums it.  Lets a large system   */
+/* be checked on a sample of its bodies.                                     */
+ORC_EXPORT void orc_forces_aos_idx(float *force, const float *posMass, float eps2, size_t N,
+                                   const long long *idx, size_t n_targets)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(guided)
+#endif
+    for (long long tt = 0; tt < (long long)n_targets; tt++) {
+        size_t i = (size_t)idx[tt];
+        const float myX = posMass[4 * i + 0];
+        const float myY = posMass[4 * i + 1];
+        const float myZ = posMass[4 * i + 2];
+        float acx = 0, acy = 0, acz = 0;
+#if defined(_OPENMP) && defined(ORC_FAST)
+#pragma omp simd reduction(+ : acx, acy, acz)
+#endif
+        for (size_t j = 0; j < N; j++) {
+            float fx, fy, fz;
+            orc_body_body(&fx, &fy, &fz, myX, myY, myZ,
+                          posMass[4 * j + 0], posMass[4 * j + 1],
+                          posMass[4 * j + 2], posMass[4 * j + 3], eps2);
+            acx += fx;
+            acy += fy;
+            acz += fz;
+        }
+        force[4 * tt + 0] = acx;
+        force[4 * tt + 1] = acy;
+        force[4 * tt + 2] = acz;
+        force[4 * tt + 3] = 0.0f;
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* CPU_SOA: src/nbody_CPU_SOA.cpp:53-105.  pos[3][N], mass[N], force[3][N].  */
 /* This is the reference's timed CPU path.  i_begin/i_end restrict the       */
@@ -205,6 +240,28 @@ ORC_EXPORT void orc_integrate(float *posMass, float *velInvMass, const float *fo
     }
 }
 
+/* The same step as the reference binary computes it when built with its    */
+/* own flags (meson.build:33-38: -O3 -ffast-math -march=native): GCC then    */
+/* contracts the position update pos += vel * dt into one fused multiply-add */
+/* and leaves the velocity update as written.  This form is checked bit for  */
+/* bit against the reference's compiled integrateGravitation_SOA            */
+/* (oracle/ref_shim.cpp) on this machine.                                    */
+ORC_EXPORT void orc_integrate_contracted(float *posMass, float *velInvMass, const float *force,
+                                         float dt, float damping, size_t N)
+{
+    for (size_t i = 0; i < N; i++) {
+        float invMass = velInvMass[4 * i + 3];
+        for (int c = 0; c < 3; c++) {
+            float v = velInvMass[4 * i + c];
+            v += (force[4 * i + c] * invMass) * dt;
+            v *= damping;
+            velInvMass[4 * i + c] = v;
+        }
+        for (int c = 0; c < 3; c++)
+            posMass[4 * i + c] = fmaf(velInvMass[4 * i + c], dt, posMass[4 * i + c]);
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Crosscheck metric: relError (src/nbody.cu:120-125) maxed over x,y,z of    */
 /* every body (src/nbody.cu:406-418).  The denominator is signed, so only    */
@@ -276,6 +333,95 @@ ORC_EXPORT void orc_random_unit_bodies(float *pos, float *vel, size_t N,
         vel[4 * i + 1] = v[1] * vscale;
         vel[4 * i + 2] = v[2] * vscale;
         vel[4 * i + 3] = 1.0f / pos[4 * i + 3];
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Plummer sphere (G = M = a = 1) exactly as the GB300 library's              */
+/* nbgb_ic_plummer generates it (that generator has no reference            */
+/* counterpart: the reference only draws its LCG ball).  Restated here so    */
+/* the CPU baseline can build its inputs without loading the GB300 library;  */
+/* the tests check that both produce the same bytes.  Steps: a splitmix64    */
+/* stream seeded with seed * 0x9E3779B97F4A7C15 + 7; per body a mass         */
+/* fraction x1 in (0, 0.999] gives r = (x1^(-2/3) - 1)^(-1/2); an isotropic  */
+/* direction (u uniform in [-1, 1), phi = 2 pi U[0,1)); a speed fraction q   */
+/* by von Neumann rejection on q^2 (1 - q^2)^(7/2) < 0.1 U; speed            */
+/* q sqrt(2) (1 + r^2)^(-1/4) in another isotropic direction; then the       */
+/* centre of mass and its velocity are moved to zero.  Binary64 throughout   */
+/* (built without contraction), rounded to binary32 only for posMass.        */
+/* ------------------------------------------------------------------------ */
+typedef struct { uint64_t s; } orc_splitmix;
+
+static uint64_t orc_sm_next(orc_splitmix *g)
+{
+    uint64_t z = (g->s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static double orc_sm_u01(orc_splitmix *g)
+{
+    return (double)(orc_sm_next(g) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static double orc_sm_uniform(orc_splitmix *g, double lo, double hi)
+{
+    return lo + (hi - lo) * orc_sm_u01(g);
+}
+
+static void orc_isotropic(orc_splitmix *g, double r, double *out)
+{
+    const double u = orc_sm_uniform(g, -1.0, 1.0);
+    const double ph = 2.0 * 3.14159265358979323846 * orc_sm_u01(g);
+    const double s = sqrt(fmax(0.0, 1.0 - u * u));
+    out[0] = r * s * cos(ph);
+    out[1] = r * s * sin(ph);
+    out[2] = r * u;
+}
+
+ORC_EXPORT void orc_ic_plummer(double *pos3, double *vel3, float *posMass, size_t N,
+                               uint64_t seed)
+{
+    orc_splitmix g = { seed * 0x9E3779B97F4A7C15ull + 7 };
+    double cp[3] = { 0, 0, 0 }, cv[3] = { 0, 0, 0 };
+    if (N == 0)
+        return;
+    for (size_t i = 0; i < N; i++) {
+        double x1;
+        do {
+            x1 = orc_sm_u01(&g);
+        } while (x1 <= 0.0 || x1 > 0.999);
+        const double r = 1.0 / sqrt(pow(x1, -2.0 / 3.0) - 1.0);
+        orc_isotropic(&g, r, pos3 + 3 * i);
+        double q;
+        for (;;) {
+            const double x4 = orc_sm_u01(&g), x5 = orc_sm_u01(&g);
+            const double gq = x4 * x4 * pow(1.0 - x4 * x4, 3.5);
+            if (0.1 * x5 < gq) {
+                q = x4;
+                break;
+            }
+        }
+        const double ve = sqrt(2.0) * pow(1.0 + r * r, -0.25);
+        orc_isotropic(&g, q * ve, vel3 + 3 * i);
+    }
+    for (size_t i = 0; i < N; i++)
+        for (int c = 0; c < 3; c++) {
+            cp[c] += pos3[3 * i + c];
+            cv[c] += vel3[3 * i + c];
+        }
+    for (int c = 0; c < 3; c++) {
+        cp[c] /= (double)N;
+        cv[c] /= (double)N;
+    }
+    for (size_t i = 0; i < N; i++) {
+        for (int c = 0; c < 3; c++) {
+            pos3[3 * i + c] -= cp[c];
+            vel3[3 * i + c] -= cv[c];
+            posMass[4 * i + c] = (float)pos3[3 * i + c];
+        }
+        posMass[4 * i + 3] = (float)(1.0 / (double)N);
     }
 }
 

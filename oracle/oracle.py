@@ -11,9 +11,16 @@ Function map (reference file:line each one follows):
   integrate         src/nbody.cu:158-236          (integrateOne per body)
   max_rel_error     src/nbody.cu:120-125, 406-418 (crosscheck metric)
   random_unit_bodies src/nbody_util.cpp:81-144    (LCG initial conditions)
-  ref_forces_aos / ref_forces_soa / ref_random_unit_bodies: the reference's
-                    own compiled objects (ComputeGravitation_AOS/_SOA,
-                    randomUnitBodies), only where oracle/_ref was built.
+  forces_aos_idx    src/nbody_CPU_AOS.cpp:60-95   (CPU_AOS for listed targets)
+  integrate_contracted  src/nbody.cu:158-236 as the reference's own build
+                    compiles it (position update fused)
+  ic_plummer        the GB300 library's Plummer generator, restated (inputs
+                    for the CPU baseline without loading that library)
+  ref().forces_aos / forces_soa / random_unit_bodies: the reference's own
+                    compiled objects (ComputeGravitation_AOS/_SOA,
+                    randomUnitBodies), only where oracle/_ref was built;
+  ref_driver().integrate: the reference driver's integrateGravitation_SOA
+                    (oracle/ref_shim.cpp), likewise.
 """
 from __future__ import annotations
 
@@ -32,11 +39,19 @@ _f64p = ctypes.POINTER(ctypes.c_double)
 _i64p = ctypes.POINTER(ctypes.c_longlong)
 
 
+def reference_dir() -> str | None:
+    """The reference checkout named by NBODY_REF_DIR, when it has its sources
+    (no default: machines without the reference build the restatement only)."""
+    d = os.environ.get("NBODY_REF_DIR")
+    return d if d and os.path.isdir(os.path.join(d, "src")) else None
+
+
 def build(ref: bool = False) -> None:
     """Compile the restatement (and, if asked and present, the reference)."""
     subprocess.run(["make", "-s", "-C", _HERE, "all"], check=True)
-    if ref and os.path.isdir("/root/reference/src"):
-        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+    d = reference_dir()
+    if ref and d:
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={d}"], check=True)
 
 
 def _ptr(a: np.ndarray, t):
@@ -60,12 +75,26 @@ class _Orc:
         lib.orc_random_unit_bodies.argtypes = [_f32p, _f32p, ctypes.c_size_t, ctypes.c_float,
                                                ctypes.c_float, ctypes.c_uint32]
         lib.orc_num_threads.restype = ctypes.c_int
+        lib.orc_forces_aos_idx.argtypes = [_f32p, _f32p, ctypes.c_float, ctypes.c_size_t,
+                                           _i64p, ctypes.c_size_t]
+        lib.orc_integrate_contracted.argtypes = lib.orc_integrate.argtypes
+        lib.orc_ic_plummer.argtypes = [_f64p, _f64p, _f32p, ctypes.c_size_t, ctypes.c_uint64]
         self.lib = lib
 
     def forces_aos(self, posMass: np.ndarray, eps2: float) -> np.ndarray:
         pm = np.ascontiguousarray(posMass, dtype=np.float32).reshape(-1, 4)
         out = np.zeros_like(pm)
         self.lib.orc_forces_aos(_ptr(out, _f32p), _ptr(pm, _f32p), eps2, pm.shape[0])
+        return out
+
+    def forces_aos_idx(self, posMass: np.ndarray, eps2: float, idx) -> np.ndarray:
+        """CPU_AOS sums for the listed target bodies only: (len(idx), 4)."""
+        pm = np.ascontiguousarray(posMass, dtype=np.float32).reshape(-1, 4)
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        assert idx.size == 0 or (idx.min() >= 0 and idx.max() < pm.shape[0])
+        out = np.zeros((idx.shape[0], 4), np.float32)
+        self.lib.orc_forces_aos_idx(_ptr(out, _f32p), _ptr(pm, _f32p), eps2, pm.shape[0],
+                                    _ptr(idx, _i64p), idx.shape[0])
         return out
 
     def forces_soa(self, posMass: np.ndarray, eps2: float, i_begin: int = 0,
@@ -127,6 +156,24 @@ class _Orc:
         self.lib.orc_integrate(_ptr(posMass, _f32p), _ptr(velInvMass, _f32p),
                                _ptr(force, _f32p), dt, damping, posMass.shape[0])
 
+    def integrate_contracted(self, posMass, velInvMass, force, dt: float, damping: float):
+        """As integrate, with the position update fused (fmaf), the way the
+        reference's own build (-O3 -ffast-math -march=native) compiles it."""
+        for a in (posMass, velInvMass, force):
+            assert a.dtype == np.float32 and a.flags.c_contiguous
+        self.lib.orc_integrate_contracted(_ptr(posMass, _f32p), _ptr(velInvMass, _f32p),
+                                          _ptr(force, _f32p), dt, damping, posMass.shape[0])
+
+    def ic_plummer(self, n: int, seed: int):
+        """Plummer sphere as the GB300 library's nbgb_ic_plummer makes it:
+        (pos3 float64 (n,3), vel3 float64 (n,3), posMass float32 (n,4))."""
+        p = np.zeros((n, 3), np.float64)
+        v = np.zeros((n, 3), np.float64)
+        pm = np.zeros((n, 4), np.float32)
+        self.lib.orc_ic_plummer(_ptr(p, _f64p), _ptr(v, _f64p), _ptr(pm, _f32p), n,
+                                seed % (1 << 64))
+        return p, v, pm
+
     def max_rel_error(self, force, golden) -> float:
         f = np.ascontiguousarray(force, dtype=np.float32)
         g = np.ascontiguousarray(golden, dtype=np.float32)
@@ -144,6 +191,13 @@ class _Orc:
 
 
 _cache: dict[str, object] = {}
+
+
+def fast_flags() -> str:
+    """The compiler flags of liborc_fast.so on this machine (oracle/Makefile)."""
+    import platform
+    extra = " -mlow-precision-recip-sqrt -mtune=native" if platform.machine() == "aarch64" else ""
+    return "gcc -O3 -ffast-math -fopenmp -march=native" + extra
 
 
 def ieee() -> _Orc:
@@ -219,6 +273,45 @@ class _Ref:
 
 def ref_available() -> bool:
     return os.path.exists(os.path.join(_REF, "libnbody_ref.so"))
+
+
+class _RefDriver:
+    """The reference driver's own integrator, integrateGravitation_SOA
+    (src/nbody.cu:186-236), exported by oracle/ref_shim.cpp."""
+
+    def __init__(self, path: str):
+        lib = ctypes.CDLL(path)
+        lib.ref_integrate_soa.argtypes = [_f32p] * 10 + [ctypes.c_float, ctypes.c_float,
+                                                          ctypes.c_size_t]
+        self.lib = lib
+
+    def integrate(self, posMass, velInvMass, force, dt: float, damping: float):
+        """In place on float32 (N,4) arrays (N % 1024 == 0, as the reference
+        requires), through the reference's SOA arrays."""
+        n = posMass.shape[0]
+        assert n % 1024 == 0 and n >= 1024, "the reference requires N % 1024 == 0"
+        cols = {}
+        for name, a in (("p", posMass), ("v", velInvMass), ("f", force)):
+            for c in range(4 if name != "f" else 3):
+                b = _Ref._aligned((n,))
+                b[:] = a[:, c]
+                cols[name, c] = b
+        args = [cols["p", 0], cols["p", 1], cols["p", 2], cols["v", 3], cols["v", 0],
+                cols["v", 1], cols["v", 2], cols["f", 0], cols["f", 1], cols["f", 2]]
+        self.lib.ref_integrate_soa(*(_ptr(a, _f32p) for a in args), dt, damping, n)
+        for c in range(3):
+            posMass[:, c] = cols["p", c]
+            velInvMass[:, c] = cols["v", c]
+
+
+def ref_driver_available() -> bool:
+    return os.path.exists(os.path.join(_REF, "libnbody_refdrv.so"))
+
+
+def ref_driver() -> _RefDriver:
+    if "refdrv" not in _cache:
+        _cache["refdrv"] = _RefDriver(os.path.join(_REF, "libnbody_refdrv.so"))
+    return _cache["refdrv"]
 
 
 def ref() -> _Ref:

@@ -2,8 +2,10 @@
 
 Run in a container where the reference sources are present:
 
-    make -C oracle all ref          # builds oracle/_ref/libnbody_ref.so
+    make -C oracle all ref REF=<reference checkout>   # oracle/_ref/libnbody_ref.so
     python tests/golden/gen_golden.py
+
+    python tests/golden/gen_golden.py c1_ball16384     # only the named fixtures
 
 Each fixture stores its inputs next to the outputs, so the tests need neither
 the reference nor this script.  Forces come from the reference's compiled
@@ -13,8 +15,9 @@ oracle/Makefile); reference-style initial conditions come from its compiled
 seedRandom/randomUnitBodies (src/nbody_util.cpp:81-144).  The FP64 forces are
 the oracle's own all-pairs sum.  Trajectories apply the reference's integrator
 formula (src/nbody.cu:158-182, restated in oracle/nbody_oracle.c) to the
-reference's forces, because the reference keeps its integrator static inside
-its driver.
+reference's forces; the 16,384-body case uses the reference driver's own
+compiled integrator instead (oracle/ref_shim.cpp exports the static
+integrateGravitation_SOA).
 """
 from __future__ import annotations
 
@@ -127,7 +130,35 @@ def main() -> None:
             traj[f"velInvMass{step}"] = v.copy()
     out["traj1024"] = traj
 
+    # 6. the plain single-system configuration exactly: N = 16,384 uniform in
+    #    the unit ball, m = 1/N, v = 0, eps2 = 1e-4, dt = 0.01, 10 steps with
+    #    the reference driver's own compiled integrator (integrateGravitation_SOA
+    #    through oracle/ref_shim.cpp, damping 0.95 = the driver's default,
+    #    src/nbody.cu:152) on the reference's CPU_AOS forces
+    if O.ref_driver_available():
+        n = 16384
+        pm = np.zeros((n, 4), np.float32)
+        pm[:, :3] = uniform_ball(n, 505)
+        pm[:, 3] = np.float32(1.0 / n)
+        vel = np.zeros((n, 4), np.float32)
+        vel[:, 3] = 1.0 / pm[:, 3]
+        c1 = dict(posMass0=pm.copy(), velInvMass0=vel.copy(), eps2=np.float32(1e-4),
+                  dt=np.float32(0.01), damping=np.float32(0.95))
+        p, v = pm.copy(), vel.copy()
+        for step in range(1, 11):
+            f = R.forces_aos(p, 1e-4)
+            if step == 1:
+                c1["force_aos0"] = f.copy()
+            O.ref_driver().integrate(p, v, f, 0.01, 0.95)
+            if step in (1, 10):
+                c1[f"posMass{step}"] = p.copy()
+                c1[f"velInvMass{step}"] = v.copy()
+        out["c1_ball16384"] = c1
+
+    only = set(sys.argv[1:])
     for name, d in out.items():
+        if only and name not in only:
+            continue
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **d)
         print(f"{path}: {os.path.getsize(path)} bytes")

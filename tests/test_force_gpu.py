@@ -118,14 +118,25 @@ def test_plain_16k_case(cuda):
 
 
 def test_million_body_plummer_properties(cuda):
-    """N = 1,048,576 Plummer sphere: FP64 subsample, Newton's third law,
-    exact mass scaling, determinism."""
+    """N = 1,048,576 Plummer sphere: FP64 and CPU_AOS on a subsample,
+    Newton's third law, exact mass scaling, determinism."""
     n = 1 << 20
     _, _, pm, _ = nb.ic_plummer(n, 20)
     out = _gpu_force(pm, 1e-4)
     idx = np.random.default_rng(1).choice(n, 512, replace=False)
-    mx, rms = nb.force_error_stats(out, _f64_as4(pm, 1e-4, idx)[:, :3], idx)
+    f64 = _f64_as4(pm, 1e-4, idx)
+    mx, rms = nb.force_error_stats(out, f64[:, :3], idx)
     assert mx <= TOL_VS_FP64 and rms <= RMS_VS_FP64, (mx, rms)
+    # the gate against the reference's CPU_AOS (src/nbody_CPU_AOS.cpp:51-98)
+    # at this size, on the same targets: directly against the IEEE
+    # restatement (sequential j sum), and against the restatement built with
+    # the reference's own flags (its vectorised j sum; on aarch64 its
+    # -mlow-precision-recip-sqrt pair terms are themselves up to ~6e-5 from
+    # FP64, so that build is gated net of its own distance from FP64)
+    ref_ieee = O.ieee().forces_aos_idx(pm, 1e-4, idx)
+    assert O.per_body_rel_error(out[idx], ref_ieee)[0] <= TOL_VS_REFERENCE
+    ref_fast = O.fast().forces_aos_idx(pm, 1e-4, idx)
+    assert _within_reference(out[idx], ref_fast, f64)
     # total momentum change sum_i m_i F_i vanishes (pairwise antisymmetry)
     m = pm[:, 3:4].astype(np.float64)
     tot = (m * out[:, :3]).sum(0)

@@ -37,3 +37,33 @@ def test_integrate_reference_reproduces_golden_step(cuda):
     torch.cuda.synchronize()
     assert np.array_equal(tp.cpu().numpy(), t["posMass1"])
     assert np.array_equal(tv.cpu().numpy(), t["velInvMass1"])
+
+
+@pytest.mark.parametrize("n", [1001, 4096])
+def test_kdk_step_is_the_fp64_leapfrog(cuda, n):
+    """One FP64 kick-drift-kick step on the GPU (kick+drift kernel, force pass,
+    half-kick kernel) against the same leapfrog evaluated on the host in FP64
+    with the GPU's own accelerations: equal to FP64 rounding (the GPU fuses
+    each update into one multiply-add).  The FP32 posMass the next force pass
+    reads is the FP64 position rounded, with the mass; odd N covers the
+    kernels' last, half-filled body pair."""
+    import torch
+    p, v, pm, _ = nb.ic_plummer(n, 31)
+    m = pm[:, 3].copy()
+    dt = 0.005
+    # the system's first force pass uses the same plan as nb.force: same bits
+    a0 = nb.force(torch.from_numpy(pm).cuda(), 1e-4).cpu().numpy()[:, :3].astype(np.float64)
+    s = nb.System(n, nb.INTEGRATOR_KDK64, 1e-4, dt, 1.0)
+    s.set_state64(p, v, m)
+    s.step(1)
+    p1, v1 = s.get_state64()
+    a1 = s.get_force()[:, :3].astype(np.float64)
+    pm1, _ = s.get_state()
+    s.close()
+    vh = v + a0 * (0.5 * dt)
+    xe = p + vh * dt
+    ve = vh + a1 * (0.5 * dt)
+    assert np.allclose(p1, xe, rtol=1e-14, atol=1e-16)
+    assert np.allclose(v1, ve, rtol=1e-14, atol=1e-16)
+    assert np.array_equal(pm1[:, :3], p1.astype(np.float32))
+    assert np.array_equal(pm1[:, 3], m)

@@ -68,3 +68,43 @@ def test_crosscheck_metric_semantics():
     f[1, 3] = 99.0  # w is ignored
     e = O.ieee().max_rel_error(f, g)
     assert abs(e - 0.1) < 1e-6
+
+
+def test_plain_16k_fixture_restatement():
+    """The exact plain single-system case (N = 16,384 unit ball, m = 1/N,
+    eps2 = 1e-4): the IEEE restatement of CPU_AOS is within the per-body gate
+    of the reference's own CPU_AOS forces, and the reference integrator as the
+    reference binary computes it (position update fused) reproduces the
+    reference driver's compiled integrateGravitation_SOA bit for bit."""
+    g = golden("c1_ball16384")
+    f = O.ieee().forces_aos(g["posMass0"], float(g["eps2"]))
+    assert O.per_body_rel_error(f, g["force_aos0"])[0] <= FORCE_TOL
+    p, v = g["posMass0"].copy(), g["velInvMass0"].copy()
+    O.ieee().integrate_contracted(p, v, g["force_aos0"].copy(), float(g["dt"]),
+                                  float(g["damping"]))
+    assert np.array_equal(p, g["posMass1"]) and np.array_equal(v, g["velInvMass1"])
+    # the separately rounded form differs from the compiled reference only in
+    # the position update
+    p2, v2 = g["posMass0"].copy(), g["velInvMass0"].copy()
+    O.ieee().integrate(p2, v2, g["force_aos0"].copy(), float(g["dt"]), float(g["damping"]))
+    assert np.array_equal(v2, g["velInvMass1"])
+
+
+def test_forces_for_listed_targets_match_full_sum():
+    g = golden("plummer4096")
+    idx = np.array([0, 1, 777, 4095, 2048, 777])
+    for impl in (O.ieee(), O.fast()):
+        full = impl.forces_aos(g["posMass"], float(g["eps2"]))
+        part = impl.forces_aos_idx(g["posMass"], float(g["eps2"]), idx)
+        assert np.array_equal(part[:, :3], full[idx, :3])
+
+
+@pytest.mark.parametrize("n,seed", [(1, 3), (1000, 20260), (4097, 2 ** 61 + 5), (65536, 9)])
+def test_plummer_restatement_is_byte_identical(n, seed):
+    """The CPU baseline builds its Plummer inputs with the oracle's
+    restatement of the library's generator, without loading the library:
+    both must give the same bytes."""
+    import nbody_gb300 as nb
+    p, v, pm = O.ieee().ic_plummer(n, seed)
+    p2, v2, pm2, _ = nb.ic_plummer(n, seed)
+    assert np.array_equal(p, p2) and np.array_equal(v, v2) and np.array_equal(pm, pm2)

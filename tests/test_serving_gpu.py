@@ -32,6 +32,36 @@ def test_results_identical_alone_and_in_the_mix(cuda):
             assert np.array_equal(a, b), r["id"]
 
 
+def test_main_lane_results_alone_and_in_the_mix(cuda):
+    """Requests above the express lane's size limit (N in [8,193, 40,000])
+    run in the main lane; those with N >= 16,384 are evaluated there by the
+    Newton's-third-law block-pair launch, whose per-body sums are FP64
+    atomics.  One-sided systems must come out bit-identical alone and in the
+    mix; Newton-3 systems repeat to FP64 summation order (an FP32
+    acceleration can differ by one rounding where an FP64 sum lies on an FP32
+    rounding boundary), so their states must agree to 1e-6 of their scale."""
+    reqs = serving.make_requests(8, 400.0, 17, n_lo=8193, n_hi=40000, steps_lo=5,
+                                 steps_hi=20)
+    assert any(r["n"] >= 16384 for r in reqs) and any(r["n"] < 16384 for r in reqs)
+    keep = {r["id"] for r in reqs}
+    srv = serving.BatchedServer(1e-4, 0.005, 2e9, 8)
+    recs, mixed, info = srv.run(reqs, keep_states=keep)
+    srv.close()
+    assert all("latency" in r for r in recs.values())
+    assert info["lanes"]["main"]["requests"] == len(reqs)
+    for r in reqs:
+        s = serving.BatchedServer(1e-4, 0.005, 2e9, 1)
+        _, alone, _ = s.run([dict(r, arrival=0.0)], keep_states={r["id"]})
+        s.close()
+        a_st, m_st = alone[r["id"]], mixed[r["id"]]
+        if r["n"] < 16384:
+            for a, b in zip(a_st, m_st):
+                assert np.array_equal(a, b), r["id"]
+        else:
+            for a, b in zip(a_st[:2], m_st[:2]):  # positions, velocities
+                assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max(), r["id"]
+
+
 def test_tiny_budget_admits_within_limits(cuda):
     reqs = _stream(10, float("inf"), 4)
     biggest = max(r["n"] for r in reqs) * serving.BYTES_PER_BODY

@@ -19,8 +19,10 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 # per-body |dF|/|F| between two evaluations of the same sum (they may use
-# different j-splits, so they differ in rounding only)
+# different j-splits, so they differ in rounding only), and against the FP64
+# all-pairs sum (the gate of the other force tests)
 TOL = 1e-5
+TOL_VS_FP64 = 5e-6
 
 
 def _c_abi():
@@ -64,6 +66,60 @@ def test_static_scratch_matches_allocating_entry_twice(cuda, n):
         assert np.all(np.isfinite(o))
         assert O.per_body_rel_error(o, r)[0] <= TOL
     assert np.array_equal(outs[0].cpu().numpy(), outs[1].cpu().numpy())
+
+
+def test_static_scratch_against_fp64_and_across_sizes(cuda):
+    """The same array serves calls of different sizes and plans in turn: a
+    100,003-body call (j-split partials and counters in use) followed by a
+    16,384-body call, each checked against the allocating entry point and
+    the FP64 all-pairs sum on a sample of bodies."""
+    import torch
+    lib = _c_abi()
+    stream = torch.cuda.current_stream().cuda_stream
+    for n in (100003, 16384, 100003):
+        _, _, pm_np, _ = nb.ic_plummer(n, 5 + n)
+        pm = torch.from_numpy(pm_np).cuda()
+        out = torch.full_like(pm, float("nan"))
+        assert lib.nbgb_force_static(out.data_ptr(), pm.data_ptr(), 1e-4, n, stream) == 0
+        wsb = lib.nbgb_force_workspace_bytes(n)
+        ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+        ref = torch.empty_like(pm)
+        assert lib.nbgb_force(ref.data_ptr(), pm.data_ptr(), 1e-4, n, ws.data_ptr(), wsb,
+                              stream) == 0
+        torch.cuda.synchronize()
+        assert nb.last_status() == 0
+        o = out.cpu().numpy()
+        assert O.per_body_rel_error(o, ref.cpu().numpy())[0] <= TOL
+        idx = np.random.default_rng(n).choice(n, 256, replace=False)
+        f64 = O.ieee().forces_f64(pm_np, float(np.float32(1e-4)), idx)
+        t = np.zeros((idx.size, 4))
+        t[:, :3] = f64
+        assert O.per_body_rel_error(o[idx], t)[0] <= TOL_VS_FP64
+
+
+@pytest.mark.parametrize("delta", [0, 1])
+def test_static_scratch_at_its_documented_limit(cuda, delta):
+    """N = capacity / 16 (and one less, padded to the same tiles) is accepted
+    and evaluated; spot checks against the allocating entry point."""
+    import torch
+    lib = _c_abi()
+    n = lib.nbgb_force_static_capacity_bytes() // 16 - delta
+    stream = torch.cuda.current_stream().cuda_stream
+    _, _, pm_np, _ = nb.ic_plummer(n, 99)
+    pm = torch.from_numpy(pm_np).cuda()
+    out = torch.full_like(pm, float("nan"))
+    assert lib.nbgb_force_static(out.data_ptr(), pm.data_ptr(), 1e-4, n, stream) == 0
+    wsb = lib.nbgb_force_workspace_bytes(n)
+    ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+    ref = torch.empty_like(pm)
+    assert lib.nbgb_force(ref.data_ptr(), pm.data_ptr(), 1e-4, n, ws.data_ptr(), wsb,
+                          stream) == 0
+    torch.cuda.synchronize()
+    assert nb.last_status() == 0
+    o = out.cpu().numpy()
+    assert np.all(np.isfinite(o))
+    idx = np.random.default_rng(3).choice(n, 4096, replace=False)
+    assert O.per_body_rel_error(o[idx], ref.cpu().numpy()[idx])[0] <= TOL
 
 
 def test_static_scratch_rejects_sizes_beyond_its_limit(cuda):
