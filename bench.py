@@ -430,10 +430,11 @@ def integrate_roofline(n, kd_ms, hk_ms):
 
 def force_accuracy(pm: np.ndarray, force: np.ndarray, k: int = 1024, seed: int = 7):
     """Per-body |F - T| / |T| of `force` on a seeded sample of k bodies: T the
-    FP64 all-pairs sum of the same FP32 inputs, and the CPU_AOS restatement
-    (src/nbody_CPU_AOS.cpp:51-98) built IEEE (sequential sum) and with the
-    reference's flags.  The reference-flag build is also given net of its
-    own distance from FP64 (its aarch64 reciprocal square root is
+    FP64 all-pairs sum of the same FP32 inputs; the reference's compiled
+    CPU_AOS (src/nbody_CPU_AOS.cpp:51-98) from its fixture; and the CPU_AOS
+    restatement built on this host IEEE (sequential sum: at N = 2^20 itself
+    ~1e-4 from FP64) and with the reference's flags (given also net of its
+    own distance from FP64: on aarch64 its reciprocal square root is
     low-precision)."""
     from oracle import oracle as O
     n = pm.shape[0]
@@ -449,14 +450,29 @@ def force_accuracy(pm: np.ndarray, force: np.ndarray, k: int = 1024, seed: int =
     fast = O.fast().forces_aos_idx(pm, EPS2, idx)[:, :3].astype(np.float64)
     net = (np.linalg.norm(f - fast, axis=1) - np.linalg.norm(fast - t64, axis=1)) / \
         np.linalg.norm(fast, axis=1)
-    return {"sample": f"{idx.size} seeded bodies of the N={n:,} input, forces of the "
-                      "drop-in call (e2e leg)",
-            "vs_fp64": stats(t64), "vs_cpu_aos_ieee": stats(ieee),
+    out = {"sample": f"{idx.size} seeded bodies of the N={n:,} input, forces of the "
+                     "drop-in call (e2e leg)",
+           "vs_fp64": stats(t64)}
+    # the reference's own compiled CPU_AOS on this input, when its forces for
+    # this sample are on file (made where the reference builds)
+    fx = os.path.join(ROOT, "tests", "golden", "c2_plummer1m_sample.npz")
+    if os.path.exists(fx):
+        import hashlib
+        g = np.load(fx)
+        if (int(g["n"]) == n and np.array_equal(g["idx"], idx) and
+                hashlib.sha256(np.ascontiguousarray(pm).tobytes()).hexdigest() ==
+                g["posMass_sha256"].item().decode()):
+            out["vs_reference_compiled_cpu_aos"] = dict(
+                stats(g["force_aos"][:, :3].astype(np.float64)),
+                source="tests/golden/c2_plummer1m_sample.npz (the reference's "
+                       "ComputeGravitation_AOS built with its flags on x86-64)")
+    return dict(out, **{
+            "vs_cpu_aos_ieee": stats(ieee),
             "vs_cpu_aos_reference_flags": dict(stats(fast),
                                                net_of_own_fp64_distance_max=float(
                                                    max(0.0, net.max())),
                                                flags=O.fast_flags()),
-            "gates": {"vs_reference_max": 1e-5, "vs_fp64_max": 5e-6}}
+            "gates": {"vs_reference_max": 1e-5, "vs_fp64_max": 5e-6}})
 
 
 def measure_newton3(args, n, p3, v3, pm_np, dev, ffma, ffma2, fp32_peak, flush):

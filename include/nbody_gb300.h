@@ -103,6 +103,22 @@ NBGB_API int nbgb_force_ex(float *force, const float *posMass, float softeningSq
  * accumulated in FP64 and rounded to FP32 at the end.  Same arguments and
  * conventions as nbgb_force; workspace >= nbgb_force_newton3_workspace_bytes.
  */
+/*
+ * Replaces: one GPU's share of the reference's multi-GPU algorithm
+ * (ComputeGravitation_multiGPU / ComputeNBodyGravitation_multiGPU,
+ * src/nbody_multiGPU.cu:47-125): the forces on target rows
+ * [row_begin, row_end) of posMass against all N sources.  posMass: DEVICE,
+ * all N bodies (replicated on every GPU, as the reference copies it to
+ * each); force_rows: DEVICE float4[row_end - row_begin].  Unlike the
+ * reference, any split of the rows is accepted (it requires N % GPUs == 0).
+ * Workspace: nbgb_force_rows_workspace_bytes(N, rows), 256-byte aligned.
+ * Stream-ordered.  nbody_gb300.sharded drives one rank per GPU with it.
+ */
+NBGB_API size_t nbgb_force_rows_workspace_bytes(size_t N, size_t rows);
+NBGB_API int nbgb_force_rows(float *force_rows, const float *posMass, float softeningSquared,
+                             size_t N, size_t row_begin, size_t row_end, void *workspace,
+                             size_t workspace_bytes, void *stream);
+
 NBGB_API size_t nbgb_force_newton3_workspace_bytes(size_t N);
 NBGB_API int nbgb_force_newton3(float *force, const float *posMass, float softeningSquared,
                                 size_t N, void *workspace, size_t workspace_bytes, void *stream);

@@ -141,6 +141,28 @@ def force(posMass, softeningSquared: float, out=None, stream=None, workspace: Wo
     return out
 
 
+def force_rows(posMass, softeningSquared: float, row_begin: int, row_end: int, out=None,
+               stream=None, workspace: Workspace = None):
+    """Forces on the target rows [row_begin, row_end) of a (N,4) float32
+    CUDA tensor against all N sources (one rank's share of a row-sharded
+    evaluation, src/nbody_multiGPU.cu:47-125); returns (rows,4)."""
+    torch = _torch()
+    n = posMass.shape[0]
+    rows = row_end - row_begin
+    if out is None:
+        out = torch.empty((max(rows, 0), 4), dtype=torch.float32, device=posMass.device)
+    if rows <= 0:
+        return out
+    lib = load()
+    wsb = lib.nbgb_force_rows_workspace_bytes(n, rows)
+    if wsb == 0:
+        raise NbgbError(-1, "nbgb_force_rows_workspace_bytes")
+    ws = (workspace or _default_ws).get(wsb)
+    check(lib.nbgb_force_rows(_dev(out), _dev(posMass), softeningSquared, n, row_begin, row_end,
+                              ws.data_ptr(), ws.numel(), _stream(stream)), "nbgb_force_rows")
+    return out
+
+
 def force_newton3(posMass, softeningSquared: float, out=None, stream=None,
                   workspace: Workspace = None):
     """Same sum as force(), each pair evaluated once (Newton's third law)."""

@@ -38,6 +38,9 @@ SIGNATURES = {
     "nbgb_force_config_name": (ctypes.c_char_p, [ctypes.c_int]),
     "nbgb_force_set_speed": (ctypes.c_int, [ctypes.c_int, ctypes.c_double]),
     "nbgb_force_get_speed": (ctypes.c_double, [ctypes.c_int]),
+    "nbgb_force_rows_workspace_bytes": (c_size, [c_size, c_size]),
+    "nbgb_force_rows": (ctypes.c_int, [c_vp, c_vp, ctypes.c_float, c_size, c_size, c_size, c_vp,
+                                       c_size, c_vp]),
     "nbgb_force_static": (ctypes.c_int, [c_vp, c_vp, ctypes.c_float, c_size, c_vp]),
     "nbgb_force_static_capacity_bytes": (c_size, []),
     "nbgb_integrate_reference": (ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_float,

@@ -527,6 +527,14 @@ static const ForceConfig kConfigs[] = {
     NBGB_CFG(8, 3, 1024, 2, 6, 4, 2, "log4"),  // 33: as 27, 3 targets per thread
     NBGB_CFG(8, 3, 512, 3, 6, 4, 2, "log4"),   // 34: as 28, 3 targets per thread
     NBGB_CFG(8, 2, 2048, 2, 6, 4, 2, "log4"),  // 35: as 27, 2048-body tiles
+    NBGB_CFG(6, 2, 1024, 2, 6, 4, 3, "log4"),  // 36: as 27, 6 warps x 3 CTAs/SM (18 warps)
+    NBGB_CFG(9, 2, 1024, 2, 6, 4, 2, "log4"),  // 37: as 27, 9 warps x 2 CTAs/SM (18 warps)
+    NBGB_CFG(5, 2, 1024, 2, 6, 4, 4, "log4"),  // 38: as 27, 5 warps x 4 CTAs/SM (20 warps)
+    NBGB_CFG(6, 2, 2048, 2, 6, 4, 3, "log4"),  // 39: as 36, 2048-body tiles
+    NBGB_CFG(6, 3, 1024, 2, 6, 4, 2, "log4"),  // 40: 3 targets per thread, 12 warps
+    NBGB_CFG(7, 2, 1024, 2, 6, 4, 3, "log4"),  // 41: as 27, 7 warps x 3 CTAs/SM (21 warps)
+    NBGB_CFG(10, 2, 1024, 2, 6, 4, 2, "log4"), // 42: as 27, 10 warps x 2 CTAs/SM (20 warps)
+    NBGB_CFG(4, 2, 1024, 2, 6, 4, 5, "log4"),  // 43: as 27, 4 warps x 5 CTAs/SM (20 warps)
 };
 static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
 // Relative throughput of each configuration (interactions/s per resident
@@ -537,7 +545,8 @@ static double g_speed[] = {
     0.943, 0.934, 0.981, 0.970, 0.902, 0.981, 0.955, 0.954, 0.962, 0.973,  // 0-9
     0.990, 0.966, 0.873, 0.936, 0.987, 0.981, 0.981, 0.982, 0.981, 0.928,  // 10-19
     0.987, 0.951, 0.974, 0.900, 0.997, 1.000, 0.977, 1.057, 1.030, 1.026,  // 20-29
-    1.034, 1.009, 1.016, 0.997, 1.020, 1.057,                              // 30-35
+    1.034, 1.009, 1.016, 0.997, 1.020, 1.057, 1.000, 1.000, 1.000, 1.000,  // 30-39
+    1.000, 1.000, 1.000, 1.000,                                            // 40-43
 };
 static_assert(sizeof(g_speed) / sizeof(g_speed[0]) == sizeof(kConfigs) / sizeof(kConfigs[0]),
               "one speed per configuration");
@@ -597,15 +606,17 @@ static const DeviceInfo *device_info() {
     return &d;
 }
 
-static void fill_layout(ForcePlan &pl, size_t n) {
+// n sources; nt targets (0: the same n bodies).
+static void fill_layout(ForcePlan &pl, size_t n, size_t nt = 0) {
     const ForceConfig &cf = kConfigs[pl.config];
     const size_t bi = (size_t)cf.warps * 32 * cf.k;
     pl.n = n;
+    pl.nt = nt;
     pl.block_bodies = (int)bi;
     pl.tile_bodies = cf.jt;
     pl.js_vpb = cf.mode == 4 ? 2 : 1;
     pl.js_log = cf.mode == 6 ? 1 : 0;
-    pl.nblocks = (int)((n + bi - 1) / bi);
+    pl.nblocks = (int)(((nt ? nt : n) + bi - 1) / bi);
     pl.ntiles = (int)((n + cf.jt - 1) / cf.jt);
     pl.ni_pad = (size_t)pl.nblocks * bi;
     pl.off_js = 0;
@@ -628,7 +639,7 @@ static void fill_layout(ForcePlan &pl, size_t n) {
 // interaction throughput is assumed equal across configurations.  The chosen
 // plan minimises waves x per-unit time.
 static int plan_force_among(size_t n, const std::vector<int> &cands, int force_nsplit,
-                            ForcePlan &pl) {
+                            ForcePlan &pl, size_t nt = 0) {
     const DeviceInfo *d = device_info();
     if (!d)
         return NBGB_ERR_CUDA;
@@ -641,7 +652,7 @@ static int plan_force_among(size_t n, const std::vector<int> &cands, int force_n
             continue;
         const double slots = (double)d->sms * occ;
         const long long bi = (long long)cf.warps * 32 * cf.k;
-        const long long nb = ((long long)n + bi - 1) / bi;
+        const long long nb = ((long long)(nt ? nt : n) + bi - 1) / bi;
         const long long ntl = ((long long)n + cf.jt - 1) / cf.jt;
         int s_lo = 1, s_hi = (int)std::min<long long>(ntl, 256);
         if (force_nsplit > 0)
@@ -666,7 +677,7 @@ static int plan_force_among(size_t n, const std::vector<int> &cands, int force_n
         return NBGB_ERR_UNSUPPORTED;
     pl.config = best_c;
     pl.nsplit = best_s;
-    fill_layout(pl, n);
+    fill_layout(pl, n, nt);
     return NBGB_OK;
 }
 
@@ -682,6 +693,15 @@ int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
         cands.assign(std::begin(kDefaultCandidates), std::end(kDefaultCandidates));
     }
     return plan_force_among(n, cands, force_nsplit, pl);
+}
+
+int plan_force_rows(size_t n, size_t rows, ForcePlan &pl) {
+    if (n == 0 || n > kMaxBodies || rows == 0 || rows > n)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    return plan_force_among(n,
+                            std::vector<int>(std::begin(kDefaultCandidates),
+                                             std::end(kDefaultCandidates)),
+                            -1, pl, rows);
 }
 
 int plan_force_rsqrt(size_t n, ForcePlan &pl) {
@@ -747,7 +767,7 @@ int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, cons
     p.part_hi = pl.nsplit > 1 ? (float4 *)(ws + pl.off_hi) : nullptr;
     p.part_lo = pl.nsplit > 1 ? (float4 *)(ws + pl.off_lo) : nullptr;
     p.counters = pl.nsplit > 1 ? (unsigned *)(ws + pl.off_cnt) : nullptr;
-    p.n = (int)pl.n;
+    p.n = (int)plan_targets(pl);
     p.ntiles = pl.ntiles;
     p.nsplit = pl.nsplit;
     p.ni_pad = (int)pl.ni_pad;
@@ -936,6 +956,40 @@ NBGB_API int nbgb_force(float *force, const float *posMass, float softeningSquar
                         void *workspace, size_t workspace_bytes, void *stream) {
     return nbgb_force_ex(force, posMass, softeningSquared, N, workspace, workspace_bytes, -1, -1,
                          stream);
+}
+
+NBGB_API size_t nbgb_force_rows_workspace_bytes(size_t N, size_t rows) {
+    ForcePlan pl;
+    if (plan_force_rows(N, rows, pl) != NBGB_OK)
+        return 0;
+    return pl.workspace_bytes;
+}
+
+// Forces on the target rows [row_begin, row_end) of posMass against all N
+// sources: one rank's share of a row-sharded evaluation.
+NBGB_API int nbgb_force_rows(float *force_rows, const float *posMass, float softeningSquared,
+                             size_t N, size_t row_begin, size_t row_end, void *workspace,
+                             size_t workspace_bytes, void *stream) {
+    if (row_end < row_begin || row_end > N)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (row_end == row_begin)
+        return NBGB_OK;
+    if (!force_rows || !posMass)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    if (((uintptr_t)force_rows | (uintptr_t)posMass) & 15u)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    ForcePlan pl;
+    int rc = plan_force_rows(N, row_end - row_begin, pl);
+    if (rc != NBGB_OK)
+        return rc;
+    if (!workspace || workspace_bytes < pl.workspace_bytes || ((uintptr_t)workspace & 255u))
+        return NBGB_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = launch_pack(pl, (const float4 *)posMass, workspace, st);
+    if (rc != NBGB_OK)
+        return rc;
+    return launch_force(pl, (float4 *)force_rows, (const float4 *)posMass + row_begin, nullptr,
+                        softeningSquared, workspace, st);
 }
 
 NBGB_API float ComputeGravitation_GPU_GB300(float *force, float *posMass, float softeningSquared,

@@ -21,7 +21,8 @@ int current_context(int *device, unsigned long long *ctx_id);
 struct ForcePlan {
     int config = 0;       // index into the kernel configuration table
     int nsplit = 1;       // j-slices per i-block
-    size_t n = 0;         // bodies
+    size_t n = 0;         // bodies (sources; also the targets unless nt says otherwise)
+    size_t nt = 0;        // target bodies (rows) when they are a slice: 0 = n
     int block_bodies = 0; // targets per CTA (BI)
     int tile_bodies = 0;  // sources per shared-memory tile (JT)
     int nblocks = 0;      // i-blocks
@@ -38,6 +39,10 @@ int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl);
 // (for masses < 0, which have no logarithm).
 int plan_force_rsqrt(size_t n, ForcePlan &pl);
 int plan_force_within(size_t n, size_t max_bytes, ForcePlan &pl);
+// Plan for `rows` target bodies (a contiguous slice of the n bodies) against
+// all n sources; launch_force then takes the slice's first body as posMass.
+int plan_force_rows(size_t n, size_t rows, ForcePlan &pl);
+inline size_t plan_targets(const ForcePlan &pl) { return pl.nt ? pl.nt : pl.n; }
 int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream);
 // jstream == nullptr: use the j-stream inside the workspace.
 int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,

@@ -155,6 +155,24 @@ def main() -> None:
                 c1[f"velInvMass{step}"] = v.copy()
         out["c1_ball16384"] = c1
 
+    # 7. the plain large system's input (N = 1,048,576 Plummer, the bench's
+    #    seed), forces of the reference's compiled CPU_AOS on every body, kept
+    #    for a seeded 1,024-body sample (the bench's accuracy sample) with
+    #    their FP64 sums; the input itself is regenerated by the tests from
+    #    its seed (oracle restatement of the library's Plummer generator) and
+    #    checked against the stored checksum
+    if os.environ.get("NBODY_GOLDEN_LARGE") or "c2_plummer1m_sample" in sys.argv[1:]:
+        import hashlib
+        n, seed = 1 << 20, 20260
+        _, _, pm = O.ieee().ic_plummer(n, seed)
+        idx = np.random.default_rng(7).choice(n, 1024, replace=False)
+        fa = R.forces_aos(pm, 1e-4)
+        out["c2_plummer1m_sample"] = dict(
+            n=np.int64(n), seed=np.int64(seed), eps2=np.float32(1e-4), idx=idx.astype(np.int64),
+            posMass_sha256=np.bytes_(hashlib.sha256(pm.tobytes()).hexdigest().encode()),
+            posMass_idx=pm[idx].copy(), force_aos=fa[idx].copy(),
+            force_f64=O.ieee().forces_f64(pm, float(np.float32(1e-4)), idx))
+
     only = set(sys.argv[1:])
     for name, d in out.items():
         if only and name not in only:

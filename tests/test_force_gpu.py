@@ -71,8 +71,8 @@ def test_drop_in_entry_matches_reference(cuda, case):
     assert np.isfinite(nb.crosscheck_max_rel_error(out, g["force_aos"]))
 
 
-NUM_CONFIGS = 36
-LOG_DOMAIN_CONFIGS = range(27, 36)  # every fourth source pair in the log domain
+NUM_CONFIGS = 44
+LOG_DOMAIN_CONFIGS = range(27, 44)  # every fourth source pair in the log domain
 NEGATIVE_MASS = 0x8  # NBGB_STATUS_NEGATIVE_MASS
 
 
@@ -127,16 +127,14 @@ def test_million_body_plummer_properties(cuda):
     f64 = _f64_as4(pm, 1e-4, idx)
     mx, rms = nb.force_error_stats(out, f64[:, :3], idx)
     assert mx <= TOL_VS_FP64 and rms <= RMS_VS_FP64, (mx, rms)
-    # the gate against the reference's CPU_AOS (src/nbody_CPU_AOS.cpp:51-98)
-    # at this size, on the same targets: directly against the IEEE
-    # restatement (sequential j sum), and against the restatement built with
-    # the reference's own flags (its vectorised j sum; on aarch64 its
-    # -mlow-precision-recip-sqrt pair terms are themselves up to ~6e-5 from
-    # FP64, so that build is gated net of its own distance from FP64)
-    ref_ieee = O.ieee().forces_aos_idx(pm, 1e-4, idx)
-    assert O.per_body_rel_error(out[idx], ref_ieee)[0] <= TOL_VS_REFERENCE
-    ref_fast = O.fast().forces_aos_idx(pm, 1e-4, idx)
-    assert _within_reference(out[idx], ref_fast, f64)
+    # the CPU_AOS restatements built on this host, on the same targets: at
+    # this size a sequential binary32 sum over 2^20 sources (the IEEE build)
+    # is itself up to ~1e-4 from FP64, and the reference-flag build on
+    # aarch64 (-mlow-precision-recip-sqrt) up to ~2e-5, so both are gated net
+    # of their own distance from FP64; the direct gate against the
+    # reference's own compiled CPU_AOS is test_million_body_against_reference
+    for impl in (O.ieee(), O.fast()):
+        assert _within_reference(out[idx], impl.forces_aos_idx(pm, 1e-4, idx), f64)
     # total momentum change sum_i m_i F_i vanishes (pairwise antisymmetry)
     m = pm[:, 3:4].astype(np.float64)
     tot = (m * out[:, :3]).sum(0)
@@ -154,6 +152,32 @@ def test_million_body_plummer_properties(cuda):
     assert np.array_equal(r2[:, :3], 2.0 * r1[:, :3])
     # bit-identical on repeat (fixed-order combination of j-splits)
     assert np.array_equal(_gpu_force(pm, 1e-4), out)
+
+
+def test_million_body_against_reference(cuda):
+    """N = 1,048,576 Plummer sphere (the plain large system's own input):
+    the drop-in's forces against the reference's compiled CPU_AOS
+    (src/nbody_CPU_AOS.cpp:51-98, built with its flags; forces of all N
+    bodies computed when the fixture was made, a seeded 1,024-body sample
+    kept), per body, directly: max <= 1e-5; and against FP64 <= 5e-6."""
+    import hashlib
+
+    import torch
+    g = golden("c2_plummer1m_sample")
+    n, seed = int(g["n"]), int(g["seed"])
+    _, _, pm_np, _ = nb.ic_plummer(n, seed)
+    assert hashlib.sha256(pm_np.tobytes()).hexdigest() == g["posMass_sha256"].item().decode(), \
+        "this host's Plummer input differs from the fixture's"
+    pm = torch.from_numpy(pm_np).cuda()
+    f = torch.zeros_like(pm)
+    assert nb.ComputeGravitation_GPU_GB300(f, pm, float(g["eps2"]), n) > 0.0
+    out = f.cpu().numpy()[g["idx"]]
+    mx, rms = O.per_body_rel_error(out, g["force_aos"])
+    assert mx <= TOL_VS_REFERENCE, (mx, rms)
+    t64 = np.zeros((out.shape[0], 4))
+    t64[:, :3] = g["force_f64"]
+    mx64, rms64 = O.per_body_rel_error(out, t64)
+    assert mx64 <= TOL_VS_FP64 and rms64 <= RMS_VS_FP64, (mx64, rms64)
 
 
 def test_split_choice_changes_only_rounding(cuda):

@@ -108,3 +108,21 @@ def test_plummer_restatement_is_byte_identical(n, seed):
     p, v, pm = O.ieee().ic_plummer(n, seed)
     p2, v2, pm2, _ = nb.ic_plummer(n, seed)
     assert np.array_equal(p, p2) and np.array_equal(v, v2) and np.array_equal(pm, pm2)
+
+
+def test_million_body_fixture():
+    """The plain large system's input regenerates from its seed (the oracle's
+    restatement of the library's Plummer generator) to the fixture's bytes,
+    and the reference's compiled CPU_AOS forces stored for its sample are
+    within the gate of the FP64 sum and of the restatement built with the
+    reference's flags."""
+    import hashlib
+    g = golden("c2_plummer1m_sample")
+    _, _, pm = O.ieee().ic_plummer(int(g["n"]), int(g["seed"]))
+    assert hashlib.sha256(pm.tobytes()).hexdigest() == g["posMass_sha256"].item().decode()
+    assert np.array_equal(pm[g["idx"]], g["posMass_idx"])
+    ref = g["force_aos"][:, :3].astype(np.float64)
+    d = np.linalg.norm(ref - g["force_f64"], axis=1) / np.linalg.norm(g["force_f64"], axis=1)
+    assert d.max() <= FORCE_TOL
+    f = O.fast().forces_aos_idx(pm, float(g["eps2"]), g["idx"])
+    assert O.per_body_rel_error(f, g["force_aos"])[0] <= FORCE_TOL
