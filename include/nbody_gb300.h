@@ -207,8 +207,13 @@ NBGB_API int nbgb_system_set_state(nbgb_system *sys, const float *posMass,
 /* KDK only: HOST double[N][3] positions and velocities, float[N] masses. */
 NBGB_API int nbgb_system_set_state64(nbgb_system *sys, const double *pos3, const double *vel3,
                                      const float *mass);
-/* Advance nsteps (asynchronous; reference steps replay one CUDA graph). */
+/* Advance nsteps (asynchronous; steps replay one CUDA graph).  KDK: each
+   step is one kick+drift launch and one force launch; the call's closing
+   half kick is applied when the velocities are next read (getters,
+   diagnostics) or merged into the next call's opening kick. */
 NBGB_API int nbgb_system_step(nbgb_system *sys, int nsteps);
+/* KDK: apply a pending closing half kick now (asynchronous). */
+NBGB_API int nbgb_system_sync_velocities(nbgb_system *sys);
 NBGB_API int nbgb_system_set_graph(nbgb_system *sys, int enable);
 /* 0: one-sided force kernel (default); 1: Newton's-third-law variant. */
 NBGB_API int nbgb_system_set_force_algorithm(nbgb_system *sys, int algorithm);
@@ -361,6 +366,14 @@ NBGB_API const char *nbgb_status_string(int code);
    completes, gives up after limit_ms (0 < limit_ms <= 1000) and returns;
    returns the status bits it left (NBGB_STATUS_WAIT_TIMEOUT expected). */
 NBGB_API int nbgb_selftest_bounded_wait(double limit_ms);
+
+/* Checks the library's integer-pipe binary32 <-> binary64 conversions (used
+   by the FP64 integrate kernels) against the hardware conversions on n
+   pseudo-random bit patterns of every class; *mismatches receives the number
+   of differing results (0 expected).  No reference counterpart.
+   Synchronous. */
+NBGB_API int nbgb_selftest_conversions(long long n, unsigned long long seed,
+                                       unsigned long long *mismatches);
 /* Library / build identification. */
 NBGB_API const char *nbgb_version(void);
 

@@ -266,6 +266,11 @@ class System:
     def synchronize(self):
         check(self.lib.nbgb_system_synchronize(self.h), "synchronize")
 
+    def sync_velocities(self):
+        """KDK: apply the pending closing half kick now (the getters do it
+        themselves)."""
+        check(self.lib.nbgb_system_sync_velocities(self.h), "sync_velocities")
+
     def set_timing(self, enable: bool):
         check(self.lib.nbgb_system_set_timing(self.h, int(enable)), "set_timing")
 

@@ -59,6 +59,7 @@ SIGNATURES = {
     "nbgb_system_set_timing": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "nbgb_system_last_force_ms": (ctypes.c_int, [c_vp, c_f32p]),
     "nbgb_system_last_integrate_ms": (ctypes.c_int, [c_vp, c_f32p, c_f32p]),
+    "nbgb_system_sync_velocities": (ctypes.c_int, [c_vp]),
     "nbgb_system_get_state": (ctypes.c_int, [c_vp, c_f32p, c_f32p]),
     "nbgb_system_get_state64": (ctypes.c_int, [c_vp, c_f64p, c_f64p]),
     "nbgb_system_get_force": (ctypes.c_int, [c_vp, c_f32p]),
@@ -105,6 +106,8 @@ SIGNATURES = {
     "nbgb_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "nbgb_version": (ctypes.c_char_p, []),
     "nbgb_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_double]),
+    "nbgb_selftest_conversions": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_ulonglong,
+                                                 ctypes.POINTER(ctypes.c_ulonglong)]),
 }
 
 _lib = None

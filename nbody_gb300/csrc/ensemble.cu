@@ -376,9 +376,10 @@ __global__ void ens_kdk_kernel(const Desc *__restrict__ desc, const int *__restr
             if (move) {
                 const float4 a = acc[i];
                 const double kdt = 0.5 * d.dt;
-                double u = fma((double)a.x, kdt, x64[3 * stride + i]);
-                double v = fma((double)a.y, kdt, x64[4 * stride + i]);
-                double w = fma((double)a.z, kdt, x64[5 * stride + i]);
+                // conversions on the integer pipe: GB300's FP64 pipe is narrow
+                double u = fma(widen_f32(a.x), kdt, x64[3 * stride + i]);
+                double v = fma(widen_f32(a.y), kdt, x64[4 * stride + i]);
+                double w = fma(widen_f32(a.z), kdt, x64[5 * stride + i]);
                 x64[3 * stride + i] = u;
                 x64[4 * stride + i] = v;
                 x64[5 * stride + i] = w;
@@ -391,7 +392,7 @@ __global__ void ens_kdk_kernel(const Desc *__restrict__ desc, const int *__restr
                     x64[2 * stride + i] = z;
                 }
             }
-            out[h] = make_float4((float)x, (float)y, (float)z, mass[i]);
+            out[h] = make_float4(narrow_f64(x), narrow_f64(y), narrow_f64(z), mass[i]);
             if (mode == 0)
                 pm[i] = out[h];
         } else {

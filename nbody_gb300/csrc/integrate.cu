@@ -28,7 +28,12 @@
 //               v 24, a 16; write v 24)
 // Each thread owns one body pair (2q, 2q+1): FP64 components move as one
 // 16-byte double2, FP32 masses as one float2, so every access is a 128-bit
-// (or 64-bit) coalesced vector access.
+// (or 64-bit) coalesced vector access.  GB300's FP64 pipe is narrow (~1.7
+// operations per SM per clock), so the kernels keep FP64 for the updates
+// themselves (6 DFMA per body in kick_drift, 3 in half_kick) and do the
+// FP32 <-> FP64 conversions on the integer pipe (widen_f32 / narrow_f64,
+// identical results): with the hardware conversions these kernels were
+// FP64-pipe bound, not HBM bound.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -149,12 +154,12 @@ __global__ void __launch_bounds__(kIntegrateThreads)
         else
             m = make_float2(mass[i0], 0.f);
         if (kick_dt != 0.0) {
-            U.x = fma((double)a0.x, kick_dt, U.x);
-            V.x = fma((double)a0.y, kick_dt, V.x);
-            W.x = fma((double)a0.z, kick_dt, W.x);
-            U.y = fma((double)a1.x, kick_dt, U.y);
-            V.y = fma((double)a1.y, kick_dt, V.y);
-            W.y = fma((double)a1.z, kick_dt, W.y);
+            U.x = fma(widen_f32(a0.x), kick_dt, U.x);
+            V.x = fma(widen_f32(a0.y), kick_dt, V.x);
+            W.x = fma(widen_f32(a0.z), kick_dt, W.x);
+            U.y = fma(widen_f32(a1.x), kick_dt, U.y);
+            V.y = fma(widen_f32(a1.y), kick_dt, V.y);
+            W.y = fma(widen_f32(a1.z), kick_dt, W.y);
         }
         X.x = fma(U.x, drift_dt, X.x);
         Y.x = fma(V.x, drift_dt, Y.x);
@@ -169,10 +174,10 @@ __global__ void __launch_bounds__(kIntegrateThreads)
         st_d2(x64 + 3 * ld + i0, U.x, U.y);
         st_d2(x64 + 4 * ld + i0, V.x, V.y);
         st_d2(x64 + 5 * ld + i0, W.x, W.y);
-        out0 = make_float4((float)X.x, (float)Y.x, (float)Z.x, m.x);
+        out0 = make_float4(narrow_f64(X.x), narrow_f64(Y.x), narrow_f64(Z.x), m.x);
         pm[i0] = out0;
         if (two) {
-            out1 = make_float4((float)X.y, (float)Y.y, (float)Z.y, m.y);
+            out1 = make_float4(narrow_f64(X.y), narrow_f64(Y.y), narrow_f64(Z.y), m.y);
             pm[i0 + 1] = out1;
         }
     }
@@ -193,12 +198,12 @@ __global__ void __launch_bounds__(kIntegrateThreads)
     double2 U = ld_d2(u), V = ld_d2(v), W = ld_d2(w);
     const float4 a0 = accel[i0];
     const float4 a1 = two ? accel[i0 + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
-    U.x = fma((double)a0.x, kick_dt, U.x);
-    V.x = fma((double)a0.y, kick_dt, V.x);
-    W.x = fma((double)a0.z, kick_dt, W.x);
-    U.y = fma((double)a1.x, kick_dt, U.y);
-    V.y = fma((double)a1.y, kick_dt, V.y);
-    W.y = fma((double)a1.z, kick_dt, W.y);
+    U.x = fma(widen_f32(a0.x), kick_dt, U.x);
+    V.x = fma(widen_f32(a0.y), kick_dt, V.x);
+    W.x = fma(widen_f32(a0.z), kick_dt, W.x);
+    U.y = fma(widen_f32(a1.x), kick_dt, U.y);
+    V.y = fma(widen_f32(a1.y), kick_dt, V.y);
+    W.y = fma(widen_f32(a1.z), kick_dt, W.y);
     st_d2(u, U.x, U.y);
     st_d2(v, V.x, V.y);
     st_d2(w, W.x, W.y);
@@ -247,6 +252,38 @@ int launch_half_kick(double *x64, size_t ld, const float4 *accel, double kick_dt
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
+// Self-test of widen_f32 / narrow_f64 against the hardware conversions on n
+// pseudo-random bit patterns of every class (splitmix64 of the index): adds
+// the number of mismatches to *bad.
+__global__ void conversion_selftest_kernel(unsigned long long seed, long long n,
+                                           unsigned long long *bad) {
+    unsigned long long local = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long z = seed + (unsigned long long)i * 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        // exponent fields drawn across the whole range, and near the
+        // boundaries of the fast paths, half of the time
+        unsigned long long bits = z;
+        if (z & 1ull) {
+            const unsigned e = 880u + (unsigned)((z >> 1) % 290u);  // 880..1169
+            bits = (z & 0x800fffffffffffffull) | ((unsigned long long)e << 52);
+        }
+        const double d = __longlong_as_double((long long)bits);
+        const float a = narrow_f64(d), b = (float)d;
+        if (__float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b))
+            local++;
+        const float f = __uint_as_float((unsigned)(z >> 32));
+        const double wa = widen_f32(f), wb = (double)f;
+        if (__double_as_longlong(wa) != __double_as_longlong(wb) && !(wa != wa && wb != wb))
+            local++;
+    }
+    if (local)
+        atomicAdd(bad, local);
+}
+
 static NBGB_STATUS_READER(read_status_integrate_tu)
 
 int read_status_integrate(unsigned *bits) { return read_status_integrate_tu(bits); }
@@ -273,6 +310,29 @@ NBGB_API int nbgb_integrate_reference_ex(float *posMass, float *velInvMass, cons
 NBGB_API int nbgb_integrate_reference(float *posMass, float *velInvMass, const float *force,
                                       float dt, float damping, size_t N, void *stream) {
     return nbgb_integrate_reference_ex(posMass, velInvMass, force, dt, damping, N, 0, stream);
+}
+
+// Runs the conversion self-test on n patterns; *mismatches gets the count of
+// results that differ from the hardware conversions (0 expected).
+// Synchronous.
+NBGB_API int nbgb_selftest_conversions(long long n, unsigned long long seed,
+                                       unsigned long long *mismatches) {
+    if (n <= 0 || !mismatches)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    int rc = NBGB_OK;
+    if (cudaMemset(d, 0, sizeof(*d)) != cudaSuccess)
+        rc = NBGB_ERR_CUDA;
+    if (rc == NBGB_OK) {
+        nbgb::conversion_selftest_kernel<<<1024, 256>>>(seed, n, d);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(mismatches, d, sizeof(*d), cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = NBGB_ERR_CUDA;
+    }
+    cudaFree(d);
+    return rc;
 }
 
 }  // extern "C"

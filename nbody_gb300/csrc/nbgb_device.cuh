@@ -233,6 +233,47 @@ __device__ __forceinline__ void comp_add(float &hi, float &lo, float t) {
 }
 
 // ---------------------------------------------------------------------------
+// Binary32 <-> binary64 conversions on the integer pipe.
+//
+// GB300 executes FP64 arithmetic at ~1.7 operations per SM per clock, and
+// the hardware conversions cvt.f64.f32 / cvt.rn.f32.f64 run on that same
+// pipe (measured: a conversion costs as much as a DADD).  The FP64 integrate
+// kernels convert every acceleration component in and every position out,
+// so the conversions alone doubled their FP64-pipe time.  These versions do
+// the common cases with a few 32-bit integer operations and give results
+// identical to the hardware instructions; the rare cases (zero and
+// subnormal inputs to the widening, results outside the normal binary32
+// range for the narrowing, infinities and NaNs) take the hardware path.
+// ---------------------------------------------------------------------------
+
+// (double)f, exactly.  A normal binary32 (biased exponent e in 1..254) is
+// the binary64 with exponent e + 896 and its 23 mantissa bits on top.
+__device__ __forceinline__ double widen_f32(float f) {
+    const uint32_t u = __float_as_uint(f);
+    if (((u >> 23) & 0xffu) - 1u < 254u) {
+        const uint32_t hi = (((u >> 3) & 0x0fffffffu) + 0x38000000u) | (u & 0x80000000u);
+        return __hiloint2double((int)hi, (int)(u << 29));
+    }
+    return (double)f;
+}
+
+// (float)d with round-to-nearest-even, exactly.  For a biased binary64
+// exponent e in 897..1150 the result is a normal binary32 (or, when the
+// rounding carries out of the largest one, infinity, as cvt.rn gives): keep
+// the top 23 mantissa bits, round on the 29 dropped ones (ties to even).
+__device__ __forceinline__ float narrow_f64(double d) {
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    if (e - 897u < 254u) {
+        uint32_t f = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+        const uint32_t rest = lo & 0x1fffffffu;
+        f += (rest > 0x10000000u) | ((rest == 0x10000000u) & f);
+        return __uint_as_float(f);
+    }
+    return (float)d;
+}
+
+// ---------------------------------------------------------------------------
 // mbarrier and 1-D bulk copies (cp.async.bulk, the non-tensor TMA path).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {

@@ -50,6 +50,7 @@ struct nbgb_system {
     size_t ws_bytes = 0;
     bool js_valid = false;     // j-stream in ws matches pm
     bool accel_valid = false;  // KDK: force holds a(x) for the current x
+    bool v_lag = false;        // KDK: velocities trail by half a step (closing kick pending)
     bool use_graph = true;
     cudaGraphExec_t graph = nullptr;
     // optional per-launch timing of the force kernel (bypasses the graph)
@@ -166,6 +167,20 @@ int half_kick(nbgb_system *s) {
         rc = nbgb::launch_half_kick(s->x64, s->ld, s->force, 0.5 * (double)s->dt, s->n, s->stream);
     if (rc == NBGB_OK && (rc = mark(s, 3)) == NBGB_OK && s->timing)
         s->htimed = true;
+    return rc;
+}
+
+// KDK: a step leaves the velocities half a step behind the positions; the
+// closing half kick is applied only when something reads or replaces the
+// velocities, and otherwise merges into the next step's opening kick (one
+// kick of dt instead of two of dt/2).  The steady-state loop is then one
+// integrate launch and one force launch per step.
+int sync_velocities(nbgb_system *s) {
+    if (s->integrator != NBGB_INTEGRATOR_KDK64 || !s->v_lag)
+        return NBGB_OK;
+    int rc = half_kick(s);
+    if (rc == NBGB_OK)
+        s->v_lag = false;
     return rc;
 }
 
@@ -355,6 +370,7 @@ NBGB_API int nbgb_system_set_state(nbgb_system *s, const float *posMass, const f
     }
     s->js_valid = false;
     s->accel_valid = false;
+    s->v_lag = false;
     return NBGB_OK;
 }
 
@@ -388,6 +404,7 @@ NBGB_API int nbgb_system_set_state64(nbgb_system *s, const double *pos3, const d
         return NBGB_ERR_CUDA;
     s->js_valid = false;
     s->accel_valid = false;
+    s->v_lag = false;
     return NBGB_OK;
 }
 
@@ -413,14 +430,19 @@ NBGB_API int nbgb_system_step(nbgb_system *s, int nsteps) {
         }
         return NBGB_OK;
     }
-    // KDK: v(n) synchronised at entry and exit.
+    // KDK: the opening kick is a half kick when the velocities are in step
+    // with the positions, a full one when the previous call's closing half
+    // kick is still pending; the call ends with its closing half kick
+    // pending (sync_velocities).
     if (!s->accel_valid) {
         if ((rc = force_pass(s)) != NBGB_OK)
             return rc;
         s->accel_valid = true;
     }
-    if ((rc = kdk_body(s, 0.5 * (double)s->dt)) != NBGB_OK)  // first half kick + drift + force
+    const double first = s->v_lag ? (double)s->dt : 0.5 * (double)s->dt;
+    if ((rc = kdk_body(s, first)) != NBGB_OK)  // opening kick + drift + force
         return rc;
+    s->v_lag = true;
     if (nsteps > 1 && graph && (rc = build_graph(s)) != NBGB_OK)
         return rc;
     for (int k = 1; k < nsteps; k++) {
@@ -431,7 +453,15 @@ NBGB_API int nbgb_system_step(nbgb_system *s, int nsteps) {
             return rc;
         }
     }
-    return half_kick(s);
+    return NBGB_OK;
+}
+
+// KDK: apply a pending closing half kick now (the getters and diagnostics do
+// it themselves); no-op otherwise.
+NBGB_API int nbgb_system_sync_velocities(nbgb_system *s) {
+    if (!s)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    return sync_velocities(s);
 }
 
 // Force algorithm of the step loop: 0 the one-sided kernel (default), 1 the
@@ -446,6 +476,10 @@ NBGB_API int nbgb_system_set_force_algorithm(nbgb_system *s, int algorithm) {
             return NBGB_ERR_NO_MEMORY;
         }
     }
+    // the pending closing kick belongs to the old algorithm's accelerations
+    int rc = sync_velocities(s);
+    if (rc != NBGB_OK)
+        return rc;
     if (s->graph) {
         cudaGraphExecDestroy(s->graph);
         s->graph = nullptr;
@@ -513,6 +547,11 @@ NBGB_API int nbgb_system_get_state(nbgb_system *s, float *posMass, float *velInv
     if (!s)
         return NBGB_ERR_INVALID_ARGUMENT;
     const size_t n = s->n;
+    if (velInvMass) {
+        int rc = sync_velocities(s);
+        if (rc != NBGB_OK)
+            return rc;
+    }
     if (posMass &&
         cudaMemcpyAsync(posMass, s->pm, n * 16, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
         return NBGB_ERR_CUDA;
@@ -547,6 +586,11 @@ NBGB_API int nbgb_system_get_state64(nbgb_system *s, double *pos3, double *vel3)
     if (!s || s->integrator != NBGB_INTEGRATOR_KDK64)
         return NBGB_ERR_INVALID_ARGUMENT;
     const size_t n = s->n, ld = s->ld;
+    if (vel3) {
+        int rc = sync_velocities(s);
+        if (rc != NBGB_OK)
+            return rc;
+    }
     std::vector<double> h(ld * 6);
     if (cudaMemcpyAsync(h.data(), s->x64, ld * 6 * sizeof(double), cudaMemcpyDeviceToHost,
                         s->stream) != cudaSuccess ||
@@ -582,6 +626,9 @@ NBGB_API int nbgb_system_diagnostics(nbgb_system *s, double *out) {
     if (!s || !out)
         return NBGB_ERR_INVALID_ARGUMENT;
     const size_t n = s->n;
+    int sync_rc = sync_velocities(s);  // kinetic energy and momenta need v(t)
+    if (sync_rc != NBGB_OK)
+        return sync_rc;
     if (!s->diag_ws) {
         int rc = nbgb::plan_force(n, nbgb::kPotentialConfig, -1, s->diag_plan);
         if (rc != NBGB_OK)

@@ -301,6 +301,54 @@ def fifo_finish_times(arrivals, service):
     return finish
 
 
+def best_interaction_rate(n: int = 1 << 20, eps2: float = 1e-4, reps: int = 3) -> dict:
+    """The fastest force evaluation this GPU runs, in interactions/s: the
+    one-sided and the Newton's-third-law kernels on a full N = 2^20 Plummer
+    sphere (large enough that every SM is busy), best of `reps` each.  No
+    request of any size can be served faster than this rate."""
+    import torch
+
+    from . import force, force_newton3, ic_plummer
+    _, _, pm_np, _ = ic_plummer(n, 1)
+    pm = torch.from_numpy(pm_np).cuda()
+    out = {}
+    for name, fn in (("onesided", force), ("newton3", force_newton3)):
+        fn(pm, eps2)
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn(pm, eps2)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) * 1e-3)
+        out[name] = float(n) * n / best
+    out["best"] = max(out["onesided"], out["newton3"])
+    return out
+
+
+def throughput_bound(reqs, service, best_rate: float) -> dict:
+    """Upper bound of the batched server's systems/s over the plain FIFO
+    server's when both are saturated: the plain server needs sum(service);
+    no server finishes the stream faster than its total work W =
+    sum N^2 (steps + 1) at the best rate the GPU reaches on any size.  Also
+    the share of work and of plain service time per octave of N."""
+    work = np.array([float(r["n"]) ** 2 * (r["steps"] + 1) for r in reqs])
+    svc = np.asarray(service, np.float64)
+    octave = np.floor(np.log2([r["n"] for r in reqs])).astype(int)
+    rows = []
+    for o in sorted(set(octave.tolist())):
+        m = octave == o
+        rows.append({"n_range": [2 ** o, 2 ** (o + 1) - 1], "requests": int(m.sum()),
+                     "work_share": float(work[m].sum() / work.sum()),
+                     "plain_time_share": float(svc[m].sum() / svc.sum()),
+                     "plain_interactions_per_s": float(work[m].sum() / svc[m].sum())})
+    t_best = work.sum() / best_rate
+    return {"work_interactions": float(work.sum()), "best_rate_per_s": best_rate,
+            "plain_service_s": float(svc.sum()), "bound_batched_s": float(t_best),
+            "speedup_bound": float(svc.sum() / t_best), "by_octave": rows}
+
+
 def _pct(x, q):
     return float(np.percentile(np.asarray(x), q)) if len(x) else None
 
@@ -357,12 +405,15 @@ def serve_study(n_req: int = 20000, rates=(10.0,), seed: int = 5, n_lo: int = 25
         coef, *_ = np.linalg.lstsq(A, y, rcond=None)
         service = [measured.get(k, float(coef @ [1.0, r["steps"], r["steps"] * r["n"] ** 2]))
                    for k, r in enumerate(base)]
+    best = best_interaction_rate(eps2=eps2)
     out = {"study": "serving", "requests": n_req, "seed": seed, "n_range": [n_lo, n_hi],
            "steps_range": [steps_lo, steps_hi], "dt": dt, "softeningSquared": eps2,
            "budget_gb": budget_gb, "slots": slots,
            "plain_service_total_s": float(sum(service)),
            "plain_measured_requests": len(measured),
-           "plain_service_predicted": len(measured) != n_req, "by_rate": []}
+           "plain_service_predicted": len(measured) != n_req,
+           "best_rates": best, "bound": throughput_bound(base, service, best["best"]),
+           "by_rate": []}
     for rate in rates:
         reqs = make_requests(n_req, rate, seed, n_lo, n_hi, steps_lo, steps_hi)
         runs = [_batched_run(reqs, eps2, dt, budget_gb, slots, wb, sub_work, records_out,

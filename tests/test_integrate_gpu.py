@@ -1,5 +1,7 @@
 """The GPU integrator in reference mode is bit-identical to integrateOne
 (src/nbody.cu:158-182) evaluated in IEEE binary32 by the oracle."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -50,7 +52,7 @@ def test_kdk_step_is_the_fp64_leapfrog(cuda, n):
     import torch
     p, v, pm, _ = nb.ic_plummer(n, 31)
     m = pm[:, 3].copy()
-    dt = 0.005
+    dt = float(np.float32(0.005))  # the system keeps dt in binary32
     # the system's first force pass uses the same plan as nb.force: same bits
     a0 = nb.force(torch.from_numpy(pm).cuda(), 1e-4).cpu().numpy()[:, :3].astype(np.float64)
     s = nb.System(n, nb.INTEGRATOR_KDK64, 1e-4, dt, 1.0)
@@ -67,3 +69,13 @@ def test_kdk_step_is_the_fp64_leapfrog(cuda, n):
     assert np.allclose(v1, ve, rtol=1e-14, atol=1e-16)
     assert np.array_equal(pm1[:, :3], p1.astype(np.float32))
     assert np.array_equal(pm1[:, 3], m)
+
+
+def test_integer_pipe_conversions_equal_hardware(cuda):
+    """The FP64 integrate kernels convert binary32 <-> binary64 with integer
+    operations (GB300's FP64 pipe is narrow); on 2^24 random bit patterns of
+    every class, half of them near the fast paths' exponent limits, every
+    result equals the hardware conversion's."""
+    bad = ctypes.c_ulonglong(99)
+    assert nb.load().nbgb_selftest_conversions(1 << 24, 12345, ctypes.byref(bad)) == 0
+    assert bad.value == 0
