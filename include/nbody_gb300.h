@@ -350,9 +350,18 @@ NBGB_API int nbgb_force_error_stats(const float *force, const double *truth3,
    (FLOP/s, 2 per instruction), 5 = packed FMA with three varying register
    operands, 6 = packed FMA with one MUFU rsqrt per six (FLOP/s of the
    FMAs), 7 = packed and scalar FMA interleaved, 8 = the force kernel's
-   pair interaction on register-resident sources (20 FLOP/interaction).  Full-GPU launch of `iters` x 128 operations per thread, best of
-   `reps` after a warm-up.  Synchronous. */
+   pair interaction on register-resident sources (20 FLOP/interaction),
+   9 / 10 = MUFU ex2 / lg2, 11..16 = the pair interaction with some source
+   pairs in the log-domain form, 17 = FP64 FMA (FLOP/s), 18 / 19 = binary32
+   widened to binary64 plus an FP64 add (pairs/s) with the hardware / the
+   integer-pipe conversion.  Full-GPU launch of `iters` x 128 operations per
+   thread, best of `reps` after a warm-up.  Synchronous. */
 NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms);
+
+/* One streaming copy kernel moving `bytes` (half read, half written) with L2
+   evicted before each of `reps` launches: median GB/s and ms.  The measured
+   cost of a short HBM-bound kernel on this GPU.  Synchronous. */
+NBGB_API int nbgb_measure_copy(size_t bytes, int reps, double *gb_per_s, float *ms);
 
 /* ======================================================================== */
 /* Status                                                                    */

@@ -102,6 +102,7 @@ SIGNATURES = {
     "nbgb_force_error_stats": (ctypes.c_int, [c_f32p, c_f64p, c_i64p, c_size, c_f64p, c_f64p]),
     "nbgb_measure_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_f64p,
                                          c_f32p]),
+    "nbgb_measure_copy": (ctypes.c_int, [c_size, ctypes.c_int, c_f64p, c_f32p]),
     "nbgb_last_status": (ctypes.c_int, []),
     "nbgb_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "nbgb_version": (ctypes.c_char_p, []),

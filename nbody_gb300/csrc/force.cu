@@ -25,12 +25,17 @@
 //                  runs at twice the rsqrt rate on sm_103).  Every 256
 //                  sources the FP32 partial sum is
 //                  folded into a per-body compensated (TwoSum) running sum.
-//                  With nsplit > 1 the j-range of an i-block is cut into
-//                  nsplit slices so that the number of units fills the GPU's
-//                  SMs evenly.  Each unit writes its (hi, lo) partials; the
-//                  last unit of an i-block to finish (atomic counter) adds the
-//                  partials of slices 0..nsplit-1 in fixed order, so the result
-//                  does not depend on which unit finishes last.
+//                  When the i-blocks do not fill the GPU's CTA slots in whole
+//                  waves, the j-range of the last ones (or of all, for small
+//                  N) is cut into nsplit slices, so the tail of the launch is
+//                  made of shorter units that finish together: units
+//                  0..nfull-1 are whole i-blocks (launched first), the rest
+//                  are (i-block, slice) units.  Each slice writes its (hi, lo)
+//                  partials; the last slice of an i-block to finish (atomic
+//                  counter) adds the partials of slices 0..nsplit-1 in fixed
+//                  order, so the result does not depend on which finishes
+//                  last.  Splitting only the tail keeps the partials (32 B per
+//                  body and slice) small enough to stay in L2.
 //
 // The drop-in entry point ComputeGravitation_GPU_GB300 has the reference's
 // pfnComputeGravitation_AOS_t signature (src/nbody.h:68) and its conventions
@@ -56,13 +61,14 @@ struct ForceParams {
     const float4 *__restrict__ ipos;     // targets, AOS {x,y,z,m}
     const float4 *__restrict__ jstream;  // sources, paired layout, ntiles*JT bodies
     float4 *__restrict__ force;          // output {fx,fy,fz,0}
-    float4 *__restrict__ part_hi;        // [nsplit][ni_pad] (nsplit > 1 only)
-    float4 *__restrict__ part_lo;        // [nsplit][ni_pad]
-    unsigned *__restrict__ counters;     // [nblocks]
+    float4 *__restrict__ part_hi;        // [nsplit][ni_split] (split i-blocks only)
+    float4 *__restrict__ part_lo;        // [nsplit][ni_split]
+    unsigned *__restrict__ counters;     // [split i-blocks]
     int n;
     int ntiles;
     int nsplit;
-    int ni_pad;
+    int nfull;     // i-blocks 0..nfull-1 are whole units; the rest are split
+    int ni_split;  // (nblocks - nfull) * BI
     float eps2;
 };
 
@@ -139,10 +145,20 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
 
     const int tid = threadIdx.x;
     const int unit = blockIdx.x;
-    const int ib = unit / p.nsplit;
-    const int r = unit - ib * p.nsplit;
-    const int t_begin = (int)(((long long)r * p.ntiles) / p.nsplit);
-    const int t_end = (int)(((long long)(r + 1) * p.ntiles) / p.nsplit);
+    // units 0..nfull-1: whole i-blocks; then (i-block, slice) units
+    int ib, r, ns;
+    if (unit < p.nfull) {
+        ib = unit;
+        r = 0;
+        ns = 1;
+    } else {
+        const int u = unit - p.nfull;
+        ns = p.nsplit;
+        ib = p.nfull + u / ns;
+        r = u - (ib - p.nfull) * ns;
+    }
+    const int t_begin = (int)(((long long)r * p.ntiles) / ns);
+    const int t_end = (int)(((long long)(r + 1) * p.ntiles) / ns);
     const int nt = t_end - t_begin;
 
     const int lane = tid & 31;
@@ -408,7 +424,7 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     for (int k = 0; k < K; k++)
         self[k] = POT ? pm_self[k] * rsqrt_mufu(p.eps2) : 0.f;
 
-    if (p.nsplit == 1) {
+    if (ns == 1) {
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const int i = ib * BI + k * NT + tid;
@@ -420,19 +436,20 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     }
 
     // Split j-range: publish partials, the last unit of the i-block combines.
+    const int sb = ib - p.nfull;  // index among the split i-blocks
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        const size_t o = (size_t)r * p.ni_pad + (size_t)(ib * BI + k * NT + tid);
+        const size_t o = (size_t)r * p.ni_split + (size_t)(sb * BI + k * NT + tid);
         p.part_hi[o] = make_float4(hx[k], hy[k], hz[k], hp[k]);
         p.part_lo[o] = make_float4(lx[k], ly[k], lz[k], lp[k]);
     }
     __threadfence();
     __syncthreads();
     if (tid == 0) {
-        const unsigned prev = atomicAdd(&p.counters[ib], 1u);
-        s_last = (prev == (unsigned)(p.nsplit - 1));
+        const unsigned prev = atomicAdd(&p.counters[sb], 1u);
+        s_last = (prev == (unsigned)(ns - 1));
         if (s_last)
-            p.counters[ib] = 0u;  // ready for the next launch
+            p.counters[sb] = 0u;  // ready for the next launch
     }
     __syncthreads();
     if (!s_last)
@@ -444,13 +461,13 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
         if (i >= p.n)
             continue;
         float Hx = 0.f, Hy = 0.f, Hz = 0.f, Lx = 0.f, Ly = 0.f, Lz = 0.f, Hp = 0.f, Lp = 0.f;
-        for (int rr = 0; rr < p.nsplit; rr++) {
+        for (int rr = 0; rr < ns; rr++) {
             float4 h, l;
             if (rr == r) {
                 h = make_float4(hx[k], hy[k], hz[k], hp[k]);
                 l = make_float4(lx[k], ly[k], lz[k], lp[k]);
             } else {
-                const size_t o = (size_t)rr * p.ni_pad + (size_t)i;
+                const size_t o = (size_t)rr * p.ni_split + (size_t)(sb * BI + k * NT + tid);
                 h = __ldcg(p.part_hi + o);
                 l = __ldcg(p.part_lo + o);
             }
@@ -619,15 +636,18 @@ static void fill_layout(ForcePlan &pl, size_t n, size_t nt = 0) {
     pl.nblocks = (int)(((nt ? nt : n) + bi - 1) / bi);
     pl.ntiles = (int)((n + cf.jt - 1) / cf.jt);
     pl.ni_pad = (size_t)pl.nblocks * bi;
+    if (pl.nsplit == 1 || pl.nfull > pl.nblocks)
+        pl.nfull = pl.nblocks;
     pl.off_js = 0;
     size_t o = align_up((size_t)pl.ntiles * cf.jt * 16 * pl.js_vpb, 256);
-    if (pl.nsplit > 1) {
+    const size_t sbk = (size_t)split_blocks(pl);
+    if (sbk) {
         pl.off_hi = o;
-        o = align_up(o + (size_t)pl.nsplit * pl.ni_pad * 16, 256);
+        o = align_up(o + (size_t)pl.nsplit * sbk * bi * 16, 256);
         pl.off_lo = o;
-        o = align_up(o + (size_t)pl.nsplit * pl.ni_pad * 16, 256);
+        o = align_up(o + (size_t)pl.nsplit * sbk * bi * 16, 256);
         pl.off_cnt = o;
-        o = align_up(o + (size_t)pl.nblocks * 4, 256);
+        o = align_up(o + sbk * 4, 256);
     } else {
         pl.off_hi = pl.off_lo = pl.off_cnt = 0;
     }
@@ -635,22 +655,37 @@ static void fill_layout(ForcePlan &pl, size_t n, size_t nt = 0) {
 }
 
 // Cost model: units run in waves of (SMs x resident CTAs); a unit's time is
-// proportional to tiles x JT x BI x (resident CTAs per SM), i.e. the SM's
-// interaction throughput is assumed equal across configurations.  The chosen
-// plan minimises waves x per-unit time.
-static int plan_force_among(size_t n, const std::vector<int> &cands, int force_nsplit,
-                            ForcePlan &pl, size_t nt = 0) {
+// proportional to its tiles x JT x BI x (resident CTAs per SM) (plus a small
+// per-unit overhead), i.e. the SM's interaction throughput is taken as equal
+// across configurations, scaled by their measured relative speed.  For each
+// configuration and slice count s > 1 two decompositions are costed: every
+// i-block split s ways, and only the i-blocks left over after whole waves of
+// whole i-blocks split (nfull = whole waves x slots).  The cheapest wins; on
+// a tie the tail-only split, whose partial sums are far smaller.
+static double unit_time(const ForceConfig &cf, int occ, long long ntl, int s, double speed) {
+    const double bi = (double)cf.warps * 32 * cf.k;
+    return (std::ceil((double)ntl / s) * cf.jt + 64.0 + (s > 1 ? 32.0 * s : 0.0)) * bi * occ /
+           speed;
+}
+
+// Enumerates the candidate decompositions of n sources / nt targets over
+// cands; keep(plan) may reject one (e.g. a workspace limit).  The best is
+// written to pl.
+template <typename Keep>
+static int plan_enumerate(size_t n, size_t nt, const int *cands, int ncands, int force_nsplit,
+                          ForcePlan &pl, Keep keep) {
     const DeviceInfo *d = device_info();
     if (!d)
         return NBGB_ERR_CUDA;
     double best = 1e300;
-    int best_c = -1, best_s = 1;
-    for (int c : cands) {
+    bool found = false;
+    for (int ci = 0; ci < ncands; ci++) {
+        const int c = cands[ci];
         const ForceConfig &cf = kConfigs[c];
         const int occ = d->occ[c];
         if (occ <= 0)
             continue;
-        const double slots = (double)d->sms * occ;
+        const long long slots = (long long)d->sms * occ;
         const long long bi = (long long)cf.warps * 32 * cf.k;
         const long long nb = ((long long)(nt ? nt : n) + bi - 1) / bi;
         const long long ntl = ((long long)n + cf.jt - 1) / cf.jt;
@@ -658,27 +693,49 @@ static int plan_force_among(size_t n, const std::vector<int> &cands, int force_n
         if (force_nsplit > 0)
             s_lo = s_hi = (int)std::min<long long>(force_nsplit, ntl);
         for (int s = s_lo; s <= s_hi; s++) {
-            const long long units = nb * s;
-            if (units > (1ll << 31) - 1)
-                continue;
-            const double waves = std::ceil((double)units / slots);
-            const double tiles = std::ceil((double)ntl / s);
-            // + small per-unit overhead (prologue, partial write and combine)
-            const double t = waves * (tiles * cf.jt + 64.0 + (s > 1 ? 32.0 * s : 0.0)) *
-                             (double)bi * occ / g_speed[c];
-            if (t < best * (1.0 - 1e-9)) {
-                best = t;
-                best_c = c;
-                best_s = s;
+            const double t1 = unit_time(cf, occ, ntl, 1, g_speed[c]);
+            const double ts = unit_time(cf, occ, ntl, s, g_speed[c]);
+            // candidates (whole i-blocks, cost); s == 1: every block whole
+            long long opt_full[2];
+            double opt_t[2];
+            int nopt = 0;
+            if (s == 1) {
+                opt_full[nopt] = nb;
+                opt_t[nopt++] = std::ceil((double)nb / slots) * t1;
+            } else {
+                const long long whole = force_nsplit > 0 ? 0 : (nb / slots) * slots;
+                if (whole > 0 && whole < nb) {  // tail-only split first: wins ties
+                    opt_full[nopt] = whole;
+                    opt_t[nopt++] = (double)(whole / slots) * t1 +
+                                    std::ceil((double)(nb - whole) * s / slots) * ts;
+                }
+                opt_full[nopt] = 0;
+                opt_t[nopt++] = std::ceil((double)nb * s / slots) * ts;
+            }
+            for (int k = 0; k < nopt; k++) {
+                const long long units = opt_full[k] + (nb - opt_full[k]) * s;
+                if (units > (1ll << 31) - 1 || !(opt_t[k] < best * (1.0 - 1e-9)))
+                    continue;
+                ForcePlan cand;
+                cand.config = c;
+                cand.nsplit = s;
+                cand.nfull = (int)opt_full[k];
+                fill_layout(cand, n, nt);
+                if (!keep(cand))
+                    continue;
+                best = opt_t[k];
+                pl = cand;
+                found = true;
             }
         }
     }
-    if (best_c < 0)
-        return NBGB_ERR_UNSUPPORTED;
-    pl.config = best_c;
-    pl.nsplit = best_s;
-    fill_layout(pl, n, nt);
-    return NBGB_OK;
+    return found ? NBGB_OK : NBGB_ERR_UNSUPPORTED;
+}
+
+static int plan_force_among(size_t n, const std::vector<int> &cands, int force_nsplit,
+                            ForcePlan &pl, size_t nt = 0) {
+    return plan_enumerate(n, nt, cands.data(), (int)cands.size(), force_nsplit, pl,
+                          [](const ForcePlan &) { return true; });
 }
 
 int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
@@ -718,42 +775,10 @@ int plan_force_rsqrt(size_t n, ForcePlan &pl) {
 int plan_force_within(size_t n, size_t max_bytes, ForcePlan &pl) {
     if (n == 0 || n > kMaxBodies)
         return NBGB_ERR_INVALID_ARGUMENT;
-    const DeviceInfo *d = device_info();
-    if (!d)
-        return NBGB_ERR_CUDA;
-    double best = 1e300;
-    bool found = false;
-    for (int c : kDefaultCandidates) {
-        const ForceConfig &cf = kConfigs[c];
-        const int occ = d->occ[c];
-        if (occ <= 0)
-            continue;
-        const double slots = (double)d->sms * occ;
-        const long long bi = (long long)cf.warps * 32 * cf.k;
-        const long long nb = ((long long)n + bi - 1) / bi;
-        const long long ntl = ((long long)n + cf.jt - 1) / cf.jt;
-        for (int s = 1; s <= (int)std::min<long long>(ntl, 256); s++) {
-            const long long units = nb * s;
-            if (units > (1ll << 31) - 1)
-                continue;
-            ForcePlan cand;
-            cand.config = c;
-            cand.nsplit = s;
-            fill_layout(cand, n);
-            if (cand.workspace_bytes > max_bytes)
-                continue;
-            const double waves = std::ceil((double)units / slots);
-            const double tiles = std::ceil((double)ntl / s);
-            const double t = waves * (tiles * cf.jt + 64.0 + (s > 1 ? 32.0 * s : 0.0)) *
-                             (double)bi * occ / g_speed[c];
-            if (t < best * (1.0 - 1e-9)) {
-                best = t;
-                pl = cand;
-                found = true;
-            }
-        }
-    }
-    return found ? NBGB_OK : NBGB_ERR_TOO_LARGE;
+    const int rc = plan_enumerate(
+        n, 0, kDefaultCandidates, (int)(sizeof(kDefaultCandidates) / sizeof(int)), -1, pl,
+        [max_bytes](const ForcePlan &c) { return c.workspace_bytes <= max_bytes; });
+    return rc == NBGB_ERR_UNSUPPORTED ? NBGB_ERR_TOO_LARGE : rc;
 }
 
 int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,
@@ -764,17 +789,19 @@ int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, cons
     p.ipos = posMass;
     p.jstream = jstream ? jstream : (const float4 *)(ws + pl.off_js);
     p.force = force;
-    p.part_hi = pl.nsplit > 1 ? (float4 *)(ws + pl.off_hi) : nullptr;
-    p.part_lo = pl.nsplit > 1 ? (float4 *)(ws + pl.off_lo) : nullptr;
-    p.counters = pl.nsplit > 1 ? (unsigned *)(ws + pl.off_cnt) : nullptr;
+    const bool split = split_blocks(pl) > 0;
+    p.part_hi = split ? (float4 *)(ws + pl.off_hi) : nullptr;
+    p.part_lo = split ? (float4 *)(ws + pl.off_lo) : nullptr;
+    p.counters = split ? (unsigned *)(ws + pl.off_cnt) : nullptr;
     p.n = (int)plan_targets(pl);
     p.ntiles = pl.ntiles;
     p.nsplit = pl.nsplit;
-    p.ni_pad = (int)pl.ni_pad;
+    p.nfull = pl.nfull;
+    p.ni_split = split_blocks(pl) * pl.block_bodies;
     p.eps2 = eps2;
     const size_t smem = (size_t)cf.stages * cf.jt * 16 * pl.js_vpb;
     void *args[] = {&p};
-    const unsigned grid = (unsigned)((long long)pl.nblocks * pl.nsplit);
+    const unsigned grid = (unsigned)plan_units(pl);
     cudaError_t e = cudaLaunchKernel(cf.fn, dim3(grid), dim3(cf.warps * 32), args, smem, stream);
     return e == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
@@ -782,9 +809,9 @@ int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, cons
 int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream) {
     char *ws = (char *)workspace;
     float4 *js = (float4 *)(ws + pl.off_js);
-    unsigned *cnt = pl.nsplit > 1 ? (unsigned *)(ws + pl.off_cnt) : nullptr;
+    unsigned *cnt = split_blocks(pl) ? (unsigned *)(ws + pl.off_cnt) : nullptr;
     const int npad = pl.ntiles * pl.tile_bodies;
-    const int ncnt = pl.nsplit > 1 ? pl.nblocks : 0;
+    const int ncnt = split_blocks(pl);
     const int work = std::max(npad / 2, ncnt);
     const int tb = 256;
     if (pl.js_vpb == 2)

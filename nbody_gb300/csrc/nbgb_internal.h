@@ -20,7 +20,9 @@ int current_context(int *device, unsigned long long *ctx_id);
 // One force evaluation's decomposition and workspace layout.
 struct ForcePlan {
     int config = 0;       // index into the kernel configuration table
-    int nsplit = 1;       // j-slices per i-block
+    int nsplit = 1;       // j-slices of each split i-block
+    int nfull = 0;        // leading i-blocks evaluated whole (one unit each); the
+                          // rest are split nsplit ways (nsplit = 1: nfull = nblocks)
     size_t n = 0;         // bodies (sources; also the targets unless nt says otherwise)
     size_t nt = 0;        // target bodies (rows) when they are a slice: 0 = n
     int block_bodies = 0; // targets per CTA (BI)
@@ -43,6 +45,12 @@ int plan_force_within(size_t n, size_t max_bytes, ForcePlan &pl);
 // all n sources; launch_force then takes the slice's first body as posMass.
 int plan_force_rows(size_t n, size_t rows, ForcePlan &pl);
 inline size_t plan_targets(const ForcePlan &pl) { return pl.nt ? pl.nt : pl.n; }
+// i-blocks whose j-range is split (each has a partial-sum slot per slice and
+// a completion counter), and the work units of one launch
+inline int split_blocks(const ForcePlan &pl) { return pl.nsplit > 1 ? pl.nblocks - pl.nfull : 0; }
+inline long long plan_units(const ForcePlan &pl) {
+    return (long long)pl.nblocks + (long long)split_blocks(pl) * (pl.nsplit - 1);
+}
 int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream);
 // jstream == nullptr: use the j-stream inside the workspace.
 int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,

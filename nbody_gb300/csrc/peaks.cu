@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <new>
 
 #include "nbgb_device.cuh"
 #include "nbody_gb300.h"
@@ -240,9 +241,148 @@ __global__ void __launch_bounds__(256) peak_mufu_kernel(float *out, int iters) {
         out[threadIdx.x] = s;
 }
 
+// FP64 pipe: 16 independent DFMA chains per thread.
+__global__ void __launch_bounds__(256) peak_dfma_kernel(float *out, int iters, double a, double b) {
+    double x[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        x[c] = (double)(threadIdx.x + c);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int c = 0; c < kChains; c++)
+                asm volatile("fma.rn.f64 %0, %0, %1, %2;" : "+d"(x[c]) : "d"(a), "d"(b));
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        s += x[c];
+    if (s == 1234.5)
+        out[threadIdx.x] = (float)s;
+}
+
+// A binary32 widened to binary64 and added to an FP64 accumulator, 16
+// chains per thread: WIDEN 0 with the hardware conversion (cvt.f64.f32),
+// 1 with the library's integer-pipe widen_f32.  The binary32 operand is
+// advanced by one FP32 multiply per step so the conversion cannot be hoisted.
+template <int WIDEN>
+__global__ void __launch_bounds__(256) peak_widen_kernel(float *out, int iters, float g) {
+    float a[kChains];
+    double x[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; c++) {
+        a[c] = 1.0f + (float)(threadIdx.x + c) * 1e-3f;
+        x[c] = 0.0;
+    }
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int c = 0; c < kChains; c++) {
+                double w;
+                if (WIDEN == 0)
+                    asm volatile("cvt.f64.f32 %0, %1;" : "=d"(w) : "f"(a[c]));
+                else
+                    w = widen_f32(a[c]);
+                asm volatile("add.rn.f64 %0, %0, %1;" : "+d"(x[c]) : "d"(w));
+                asm volatile("mul.rn.f32 %0, %0, %1;" : "+f"(a[c]) : "f"(g));
+            }
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        s += x[c];
+    if (s == 1234.5)
+        out[threadIdx.x] = (float)s;
+}
+
+// Streaming copy (float4 per thread) and the read-only kernel that evicts L2
+// between timed copies.
+__global__ void __launch_bounds__(256) copy_f4_kernel(const float4 *__restrict__ a,
+                                                       float4 *__restrict__ b, size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n)
+        b[i] = a[i];
+}
+
+__global__ void __launch_bounds__(256) read_evict_kernel(const int4 *__restrict__ p, size_t n,
+                                                         int *sink) {
+    int4 acc = make_int4(0, 0, 0, 0);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int4 v = p[i];
+        acc.x ^= v.x;
+        acc.y ^= v.y;
+        acc.z ^= v.z;
+        acc.w ^= v.w;
+    }
+    if ((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x7fffffff)
+        *sink = 1;
+}
+
 }  // namespace nbgb
 
 extern "C" {
+
+// HBM copy rate of one kernel moving `bytes` (half read, half written) with
+// L2 evicted before each launch (a 256 MiB read): the median of `reps`
+// launches, as bytes / CUDA-event time.  Shows the fixed cost of a short
+// streaming kernel on this GPU.  Allocates its buffers; synchronous.
+NBGB_API int nbgb_measure_copy(size_t bytes, int reps, double *gb_per_s, float *ms_out) {
+    if (bytes < 32 || reps <= 0 || reps > 1000 || !gb_per_s)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const size_t n = bytes / 32;  // float4 elements copied
+    const size_t flush_bytes = (size_t)256 << 20;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    float4 *a = nullptr, *b = nullptr;
+    int4 *fl = nullptr;
+    int *sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = NBGB_ERR_CUDA;
+    float *t = new (std::nothrow) float[reps];
+    if (!t)
+        return NBGB_ERR_NO_MEMORY;
+    if (cudaMalloc(&a, n * 16) != cudaSuccess || cudaMalloc(&b, n * 16) != cudaSuccess ||
+        cudaMalloc(&fl, flush_bytes) != cudaSuccess || cudaMalloc(&sink, 4) != cudaSuccess ||
+        cudaMemset(a, 0, n * 16) != cudaSuccess || cudaMemset(fl, 0, flush_bytes) != cudaSuccess ||
+        cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        goto done;
+    for (int r = -1; r < reps; r++) {  // r = -1: warm-up
+        nbgb::read_evict_kernel<<<sms * 8, 256>>>(fl, flush_bytes / 16, sink);
+        cudaEventRecord(e0, nullptr);
+        nbgb::copy_f4_kernel<<<(unsigned)((n + 255) / 256), 256>>>(a, b, n);
+        cudaEventRecord(e1, nullptr);
+        if (cudaEventSynchronize(e1) != cudaSuccess)
+            goto done;
+        if (r >= 0 && cudaEventElapsedTime(&t[r], e0, e1) != cudaSuccess)
+            goto done;
+    }
+    for (int i = 1; i < reps; i++)  // insertion sort for the median
+        for (int j = i; j > 0 && t[j] < t[j - 1]; j--) {
+            const float x = t[j];
+            t[j] = t[j - 1];
+            t[j - 1] = x;
+        }
+    *gb_per_s = (double)n * 32 / (t[reps / 2] * 1e-3) / 1e9;
+    if (ms_out)
+        *ms_out = t[reps / 2];
+    rc = NBGB_OK;
+done:
+    delete[] t;
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    cudaFree(a);
+    cudaFree(b);
+    cudaFree(fl);
+    cudaFree(sink);
+    return rc;
+}
 
 // which: 0 = FFMA (FLOP/s), 1 = FFMA2 (FLOP/s), 2 = MUFU rsqrt (ops/s),
 //        3 = add.f32x2, 4 = mul.f32x2 (FLOP/s, 2 per instruction), 5 = FFMA2
@@ -253,10 +393,12 @@ extern "C" {
 //        9 = MUFU ex2, 10 = MUFU lg2 (ops/s), 11 / 12 = the pair
 //        interaction with 1 / 2 of every 4 source pairs in the log-domain
 //        form, 13 = 8 source pairs per step, 14..16 = 1..3 of every 8 in the
-//        log-domain form.
+//        log-domain form, 17 = DFMA (FP64 FLOP/s), 18 / 19 = binary32 widened
+//        to binary64 plus an FP64 add, with the hardware conversion / the
+//        integer-pipe widen_f32 (widen+add pairs per second).
 // Result in *rate; *ms = best launch time.  Synchronous.
 NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms_out) {
-    if (which < 0 || which > 16 || iters <= 0 || reps <= 0 || !rate)
+    if (which < 0 || which > 19 || iters <= 0 || reps <= 0 || !rate)
         return NBGB_ERR_INVALID_ARGUMENT;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -305,8 +447,14 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
             nbgb::peak_interact_kernel<8, 1><<<dim3(sms * 2), block>>>(out, iters / 16, 0.999f, 1e-3f);
         else if (which == 15)
             nbgb::peak_interact_kernel<8, 2><<<dim3(sms * 2), block>>>(out, iters / 16, 0.999f, 1e-3f);
-        else
+        else if (which == 16)
             nbgb::peak_interact_kernel<8, 3><<<dim3(sms * 2), block>>>(out, iters / 16, 0.999f, 1e-3f);
+        else if (which == 17)
+            nbgb::peak_dfma_kernel<<<grid, block>>>(out, iters, 0.999, 1e-3);
+        else if (which == 18)
+            nbgb::peak_widen_kernel<0><<<grid, block>>>(out, iters, 1.0000001f);
+        else
+            nbgb::peak_widen_kernel<1><<<grid, block>>>(out, iters, 1.0000001f);
         cudaEventRecord(e1, nullptr);
         if (cudaEventSynchronize(e1) != cudaSuccess)
             goto done;
@@ -319,7 +467,7 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
         const double threads = (double)grid.x * block.x;
         const double per_thread = (double)iters * 8 * nbgb::kChains;
         double ops = threads * per_thread;
-        if (which == 0)
+        if (which == 0 || which == 17)
             ops *= 2.0;  // FMA = 2 FLOP
         else if (which == 1 || which == 5)
             ops *= 4.0;  // two FMAs per instruction

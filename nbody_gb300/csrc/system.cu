@@ -78,9 +78,9 @@ namespace {
 
 float4 *js_of(nbgb_system *s) { return (float4 *)((char *)s->ws + s->plan.off_js); }
 unsigned *cnt_of(nbgb_system *s) {
-    return s->plan.nsplit > 1 ? (unsigned *)((char *)s->ws + s->plan.off_cnt) : nullptr;
+    return nbgb::split_blocks(s->plan) ? (unsigned *)((char *)s->ws + s->plan.off_cnt) : nullptr;
 }
-int ncnt_of(nbgb_system *s) { return s->plan.nsplit > 1 ? s->plan.nblocks : 0; }
+int ncnt_of(nbgb_system *s) { return nbgb::split_blocks(s->plan); }
 int npad_of(nbgb_system *s) { return s->plan.ntiles * s->plan.tile_bodies; }
 
 double *comp(nbgb_system *s, int c) { return s->x64 + (size_t)c * s->ld; }

@@ -180,6 +180,23 @@ def test_million_body_against_reference(cuda):
     assert mx64 <= TOL_VS_FP64 and rms64 <= RMS_VS_FP64, (mx64, rms64)
 
 
+@pytest.mark.parametrize("n", [155677, 163877, 311300])
+def test_tail_split_plans(cuda, n):
+    """Sizes whose i-blocks overflow whole waves of CTA slots: the planner
+    splits the j-range of the leftover i-blocks only (whole i-blocks first,
+    (i-block, slice) units after).  Results agree with the same
+    configuration unsplit to rounding, and with FP64 on a sample."""
+    _, _, pm, _ = nb.ic_plummer(n, n)
+    cfg, ns, _ = nb.force_plan(n)
+    out = _gpu_force(pm, 1e-4)
+    whole = _gpu_force(pm, 1e-4, config=cfg, nsplit=1)
+    assert O.per_body_rel_error(out, whole)[0] <= 1e-6
+    idx = np.random.default_rng(n).choice(n, 256, replace=False)
+    mx, rms = nb.force_error_stats(out, _f64_as4(pm, 1e-4, idx)[:, :3], idx)
+    assert mx <= TOL_VS_FP64 and rms <= RMS_VS_FP64
+    assert np.array_equal(_gpu_force(pm, 1e-4), out)  # deterministic
+
+
 def test_split_choice_changes_only_rounding(cuda):
     g = golden("ball2048")
     a = _gpu_force(g["posMass"], 1e-4, 0, 1)
