@@ -660,8 +660,9 @@ static void fill_layout(ForcePlan &pl, size_t n, size_t nt = 0) {
 // across configurations, scaled by their measured relative speed.  For each
 // configuration and slice count s > 1 two decompositions are costed: every
 // i-block split s ways, and only the i-blocks left over after whole waves of
-// whole i-blocks split (nfull = whole waves x slots).  The cheapest wins; on
-// a tie the tail-only split, whose partial sums are far smaller.
+// whole i-blocks split (nfull = whole waves x slots).  Of the plans within
+// 0.2 % of the cheapest, the one with the smallest workspace wins: the
+// tail-only split with few slices, whose partial sums stay in L2.
 static double unit_time(const ForceConfig &cf, int occ, long long ntl, int s, double speed) {
     const double bi = (double)cf.warps * 32 * cf.k;
     return (std::ceil((double)ntl / s) * cf.jt + 64.0 + (s > 1 ? 32.0 * s : 0.0)) * bi * occ /
@@ -669,16 +670,19 @@ static double unit_time(const ForceConfig &cf, int occ, long long ntl, int s, do
 }
 
 // Enumerates the candidate decompositions of n sources / nt targets over
-// cands; keep(plan) may reject one (e.g. a workspace limit).  The best is
-// written to pl.
+// cands; keep(plan) may reject one (e.g. a workspace limit).  Among the
+// candidates within kPlanTie of the cheapest, the one with the smallest
+// workspace (fewest partial sums) is written to pl.
+constexpr double kPlanTie = 2e-3;
+
 template <typename Keep>
 static int plan_enumerate(size_t n, size_t nt, const int *cands, int ncands, int force_nsplit,
                           ForcePlan &pl, Keep keep) {
     const DeviceInfo *d = device_info();
     if (!d)
         return NBGB_ERR_CUDA;
+    std::vector<std::pair<double, ForcePlan>> kept;
     double best = 1e300;
-    bool found = false;
     for (int ci = 0; ci < ncands; ci++) {
         const int c = cands[ci];
         const ForceConfig &cf = kConfigs[c];
@@ -714,7 +718,7 @@ static int plan_enumerate(size_t n, size_t nt, const int *cands, int ncands, int
             }
             for (int k = 0; k < nopt; k++) {
                 const long long units = opt_full[k] + (nb - opt_full[k]) * s;
-                if (units > (1ll << 31) - 1 || !(opt_t[k] < best * (1.0 - 1e-9)))
+                if (units > (1ll << 31) - 1 || !(opt_t[k] < best * (1.0 + kPlanTie)))
                     continue;
                 ForcePlan cand;
                 cand.config = c;
@@ -723,12 +727,19 @@ static int plan_enumerate(size_t n, size_t nt, const int *cands, int ncands, int
                 fill_layout(cand, n, nt);
                 if (!keep(cand))
                     continue;
-                best = opt_t[k];
-                pl = cand;
-                found = true;
+                best = std::min(best, opt_t[k]);
+                kept.emplace_back(opt_t[k], cand);
             }
         }
     }
+    // enumeration order decides among equal workspaces (first wins)
+    bool found = false;
+    for (const auto &e : kept)
+        if (e.first <= best * (1.0 + kPlanTie) &&
+            (!found || e.second.workspace_bytes < pl.workspace_bytes)) {
+            pl = e.second;
+            found = true;
+        }
     return found ? NBGB_OK : NBGB_ERR_UNSUPPORTED;
 }
 

@@ -277,17 +277,24 @@ __global__ void __launch_bounds__(256) peak_widen_kernel(float *out, int iters, 
     }
     for (int it = 0; it < iters; it++) {
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+        for (int u = 0; u < 8; u++) {
+            // three phases over the 16 chains, so consecutive instructions are
+            // independent and the pipes, not latencies, set the rate
+            double w[kChains];
 #pragma unroll
             for (int c = 0; c < kChains; c++) {
-                double w;
                 if (WIDEN == 0)
-                    asm volatile("cvt.f64.f32 %0, %1;" : "=d"(w) : "f"(a[c]));
+                    asm volatile("cvt.f64.f32 %0, %1;" : "=d"(w[c]) : "f"(a[c]));
                 else
-                    w = widen_f32(a[c]);
-                asm volatile("add.rn.f64 %0, %0, %1;" : "+d"(x[c]) : "d"(w));
-                asm volatile("mul.rn.f32 %0, %0, %1;" : "+f"(a[c]) : "f"(g));
+                    w[c] = widen_f32(a[c]);
             }
+#pragma unroll
+            for (int c = 0; c < kChains; c++)
+                asm volatile("add.rn.f64 %0, %0, %1;" : "+d"(x[c]) : "d"(w[c]));
+#pragma unroll
+            for (int c = 0; c < kChains; c++)
+                asm volatile("mul.rn.f32 %0, %0, %1;" : "+f"(a[c]) : "f"(g));
+        }
     }
     double s = 0.0;
 #pragma unroll
