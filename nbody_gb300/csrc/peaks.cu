@@ -262,44 +262,33 @@ __global__ void __launch_bounds__(256) peak_dfma_kernel(float *out, int iters, d
         out[threadIdx.x] = (float)s;
 }
 
-// A binary32 widened to binary64 and added to an FP64 accumulator, 16
+// A binary32 widened to binary64 and added to an FP64 accumulator, 8
 // chains per thread: WIDEN 0 with the hardware conversion (cvt.f64.f32),
 // 1 with the library's integer-pipe widen_f32.  The binary32 operand is
 // advanced by one FP32 multiply per step so the conversion cannot be hoisted.
 template <int WIDEN>
 __global__ void __launch_bounds__(256) peak_widen_kernel(float *out, int iters, float g) {
-    float a[kChains];
-    double x[kChains];
+    constexpr int C = 8;
+    float a[C];
+    double x[C];
 #pragma unroll
-    for (int c = 0; c < kChains; c++) {
+    for (int c = 0; c < C; c++) {
         a[c] = 1.0f + (float)(threadIdx.x + c) * 1e-3f;
         x[c] = 0.0;
     }
     for (int it = 0; it < iters; it++) {
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            // three phases over the 16 chains, so consecutive instructions are
-            // independent and the pipes, not latencies, set the rate
-            double w[kChains];
+        for (int u = 0; u < 16; u++)
 #pragma unroll
-            for (int c = 0; c < kChains; c++) {
-                if (WIDEN == 0)
-                    asm volatile("cvt.f64.f32 %0, %1;" : "=d"(w[c]) : "f"(a[c]));
-                else
-                    w[c] = widen_f32(a[c]);
+            for (int c = 0; c < C; c++) {
+                x[c] += WIDEN ? widen_f32(a[c]) : (double)a[c];
+                a[c] *= g;
             }
-#pragma unroll
-            for (int c = 0; c < kChains; c++)
-                asm volatile("add.rn.f64 %0, %0, %1;" : "+d"(x[c]) : "d"(w[c]));
-#pragma unroll
-            for (int c = 0; c < kChains; c++)
-                asm volatile("mul.rn.f32 %0, %0, %1;" : "+f"(a[c]) : "f"(g));
-        }
     }
     double s = 0.0;
 #pragma unroll
-    for (int c = 0; c < kChains; c++)
-        s += x[c];
+    for (int c = 0; c < C; c++)
+        s += x[c] + a[c];
     if (s == 1234.5)
         out[threadIdx.x] = (float)s;
 }
