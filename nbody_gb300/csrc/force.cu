@@ -552,6 +552,8 @@ static const ForceConfig kConfigs[] = {
     NBGB_CFG(7, 2, 1024, 2, 6, 4, 3, "log4"),  // 41: as 27, 7 warps x 3 CTAs/SM (21 warps)
     NBGB_CFG(10, 2, 1024, 2, 6, 4, 2, "log4"), // 42: as 27, 10 warps x 2 CTAs/SM (20 warps)
     NBGB_CFG(4, 2, 1024, 2, 6, 4, 5, "log4"),  // 43: as 27, 4 warps x 5 CTAs/SM (20 warps)
+    NBGB_CFG(8, 4, 1024, 2, 6, 4, 2, "log4"),  // 44: as 27, 4 targets per thread
+    NBGB_CFG(8, 2, 1024, 3, 6, 4, 2, "log4"),  // 45: as 27, 3 ring stages
 };
 static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
 // Relative throughput of each configuration (interactions/s per resident
@@ -563,7 +565,7 @@ static double g_speed[] = {
     0.990, 0.966, 0.873, 0.936, 0.987, 0.981, 0.981, 0.982, 0.981, 0.928,  // 10-19
     0.987, 0.951, 0.974, 0.900, 0.997, 1.000, 0.977, 1.057, 1.030, 1.026,  // 20-29
     1.034, 1.009, 1.016, 0.997, 1.020, 1.057, 1.000, 1.000, 1.000, 1.000,  // 30-39
-    1.000, 1.000, 1.000, 1.000,                                            // 40-43
+    1.000, 1.000, 1.000, 1.000, 1.000, 1.000,                              // 40-45
 };
 static_assert(sizeof(g_speed) / sizeof(g_speed[0]) == sizeof(kConfigs) / sizeof(kConfigs[0]),
               "one speed per configuration");
