@@ -352,9 +352,7 @@ NBGB_API int nbgb_force_error_stats(const float *force, const double *truth3,
    FMAs), 7 = packed and scalar FMA interleaved, 8 = the force kernel's
    pair interaction on register-resident sources (20 FLOP/interaction),
    9 / 10 = MUFU ex2 / lg2, 11..16 = the pair interaction with some source
-   pairs in the log-domain form, 17 = FP64 FMA (FLOP/s), 18 / 19 = binary32
-   widened to binary64 plus an FP64 add (pairs/s) with the hardware / the
-   integer-pipe conversion.  Full-GPU launch of `iters` x 128 operations per
+   pairs in the log-domain form, 17 = FP64 FMA (FLOP/s).  Full-GPU launch of `iters` x 128 operations per
    thread, best of `reps` after a warm-up.  Synchronous. */
 NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms);
 

@@ -197,14 +197,12 @@ def measure_peak(which: str, iters: int = 4096, reps: int = 5):
     register-resident pair interaction (20 FLOP/interaction) with 4 or 8
     source pairs per step: 'interact', 'interact_log1of4', 'interact_log2of4',
     'interact8', 'interact_log1of8' .. 'interact_log3of8' (that many source
-    pairs in the log-domain form); 'dfma' (FP64 FLOP/s); 'cvt_dadd' /
-    'widen_dadd' (binary32 -> binary64 conversions, hardware / integer pipe,
-    each with an FP64 add, per second)."""
+    pairs in the log-domain form); 'dfma' (FP64 FLOP/s)."""
     code = {"ffma": 0, "ffma2": 1, "mufu": 2, "fadd2": 3, "fmul2": 4, "ffma2_3op": 5,
             "ffma2_mufu": 6, "ffma2_ffma": 7, "interact": 8, "ex2": 9, "lg2": 10,
             "interact_log1of4": 11, "interact_log2of4": 12, "interact8": 13,
             "interact_log1of8": 14, "interact_log2of8": 15, "interact_log3of8": 16,
-            "dfma": 17, "cvt_dadd": 18, "widen_dadd": 19}[which]
+            "dfma": 17}[which]
     rate, ms = ctypes.c_double(), ctypes.c_float()
     check(load().nbgb_measure_peak(code, iters, reps, ctypes.byref(rate), ctypes.byref(ms)),
           "nbgb_measure_peak")

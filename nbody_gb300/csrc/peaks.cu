@@ -262,37 +262,6 @@ __global__ void __launch_bounds__(256) peak_dfma_kernel(float *out, int iters, d
         out[threadIdx.x] = (float)s;
 }
 
-// A binary32 widened to binary64 and added to an FP64 accumulator, 8
-// chains per thread: WIDEN 0 with the hardware conversion (cvt.f64.f32),
-// 1 with the library's integer-pipe widen_f32.  The binary32 operand is
-// advanced by one FP32 multiply per step so the conversion cannot be hoisted.
-template <int WIDEN>
-__global__ void __launch_bounds__(256) peak_widen_kernel(float *out, int iters, float g) {
-    constexpr int C = 8;
-    float a[C];
-    double x[C];
-#pragma unroll
-    for (int c = 0; c < C; c++) {
-        a[c] = 1.0f + (float)(threadIdx.x + c) * 1e-3f;
-        x[c] = 0.0;
-    }
-    for (int it = 0; it < iters; it++) {
-#pragma unroll
-        for (int u = 0; u < 16; u++)
-#pragma unroll
-            for (int c = 0; c < C; c++) {
-                x[c] += WIDEN ? widen_f32(a[c]) : (double)a[c];
-                a[c] *= g;
-            }
-    }
-    double s = 0.0;
-#pragma unroll
-    for (int c = 0; c < C; c++)
-        s += x[c] + a[c];
-    if (s == 1234.5)
-        out[threadIdx.x] = (float)s;
-}
-
 // Streaming copy (float4 per thread) and the read-only kernel that evicts L2
 // between timed copies.
 __global__ void __launch_bounds__(256) copy_f4_kernel(const float4 *__restrict__ a,
@@ -389,12 +358,10 @@ done:
 //        9 = MUFU ex2, 10 = MUFU lg2 (ops/s), 11 / 12 = the pair
 //        interaction with 1 / 2 of every 4 source pairs in the log-domain
 //        form, 13 = 8 source pairs per step, 14..16 = 1..3 of every 8 in the
-//        log-domain form, 17 = DFMA (FP64 FLOP/s), 18 / 19 = binary32 widened
-//        to binary64 plus an FP64 add, with the hardware conversion / the
-//        integer-pipe widen_f32 (widen+add pairs per second).
+//        log-domain form, 17 = DFMA (FP64 FLOP/s).
 // Result in *rate; *ms = best launch time.  Synchronous.
 NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, float *ms_out) {
-    if (which < 0 || which > 19 || iters <= 0 || reps <= 0 || !rate)
+    if (which < 0 || which > 17 || iters <= 0 || reps <= 0 || !rate)
         return NBGB_ERR_INVALID_ARGUMENT;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -445,12 +412,8 @@ NBGB_API int nbgb_measure_peak(int which, int iters, int reps, double *rate, flo
             nbgb::peak_interact_kernel<8, 2><<<dim3(sms * 2), block>>>(out, iters / 16, 0.999f, 1e-3f);
         else if (which == 16)
             nbgb::peak_interact_kernel<8, 3><<<dim3(sms * 2), block>>>(out, iters / 16, 0.999f, 1e-3f);
-        else if (which == 17)
-            nbgb::peak_dfma_kernel<<<grid, block>>>(out, iters, 0.999, 1e-3);
-        else if (which == 18)
-            nbgb::peak_widen_kernel<0><<<grid, block>>>(out, iters, 1.0000001f);
         else
-            nbgb::peak_widen_kernel<1><<<grid, block>>>(out, iters, 1.0000001f);
+            nbgb::peak_dfma_kernel<<<grid, block>>>(out, iters, 0.999, 1e-3);
         cudaEventRecord(e1, nullptr);
         if (cudaEventSynchronize(e1) != cudaSuccess)
             goto done;
