@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
     // (TwoSum) sum: at most 256 (128 per f32x2 half), whatever the tile size.
     constexpr int FLUSH = JT < 256 ? JT : 256;
     static_assert(JT % FLUSH == 0, "tiles hold whole flush chunks");
-    static_assert(MODE != 6 || (FLUSH % 8 == 0 && (UNROLL < 4 || UNROLL % 4 == 0)),
+    static_assert((MODE != 6 && MODE != 7) || (FLUSH % 8 == 0 && (UNROLL < 4 || UNROLL % 4 == 0)),
                   "mode 6 steps through whole groups of 4 source pairs");
 
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -331,6 +331,47 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                     comp_add(hz[k], lz[k], l + h);
                 }
                 }
+            } else if constexpr (MODE == 7) {  // as 6, next source pair loaded one ahead
+                // The operands of pair q + 1 are read from shared memory while
+                // pair q is evaluated, across group and flush boundaries, so a
+                // group never starts by waiting on its first loads.  The last
+                // pair of the tile re-reads itself instead of reaching past it.
+                f2 ax[K], ay[K], az[K];
+                ulonglong2 a = tp[0], b = tp[1];
+                for (int q0 = 0; q0 < JT / 2; q0 += FLUSH / 2) {
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    ax[k] = ay[k] = az[k] = zero2;
+                for (int q = q0; q < q0 + FLUSH / 2; q += 4) {
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int qn = min(q + u + 1, JT / 2 - 1);
+                        const ulonglong2 an = tp[2 * qn];
+                        const ulonglong2 bn = tp[2 * qn + 1];
+#pragma unroll
+                        for (int k = 0; k < K; k++) {
+                            if (u == 0)
+                                pair_interact2_log(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p,
+                                                   m15, ax[k], ay[k], az[k]);
+                            else
+                                pair_interact2(a.x, a.y, b.x, b.y, nx[k], ny[k], nz[k], eps2p,
+                                               ax[k], ay[k], az[k]);
+                        }
+                        a = an;
+                        b = bn;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    float l, h;
+                    f2_unpack(ax[k], l, h);
+                    comp_add(hx[k], lx[k], l + h);
+                    f2_unpack(ay[k], l, h);
+                    comp_add(hy[k], ly[k], l + h);
+                    f2_unpack(az[k], l, h);
+                    comp_add(hz[k], lz[k], l + h);
+                }
+                }
             } else if constexpr (MODE != 0) {  // packed f32x2 (MODE 2: all ops as FMAs)
                 f2 ax[K], ay[K], az[K];
                 for (int q0 = 0; q0 < JT / 2; q0 += FLUSH / 2) {
@@ -494,7 +535,8 @@ struct ForceConfig {
     int mode;  // 0 scalar FP32, 1 packed f32x2 (source pairs), 2 as 1 with every
                // op as an FMA, 4 packed f32x2 (target pairs, duplicated sources),
                // 5 as 1 plus the potential in w, 6 as 1 with every fourth source
-               // pair in the log domain (j-stream with log2 masses there)
+               // pair in the log domain (j-stream with log2 masses there), 7 as
+               // 6 with each source pair read one pair ahead
     const void *fn;
     const char *name;
 };
@@ -554,6 +596,8 @@ static const ForceConfig kConfigs[] = {
     NBGB_CFG(4, 2, 1024, 2, 6, 4, 5, "log4"),  // 43: as 27, 4 warps x 5 CTAs/SM (20 warps)
     NBGB_CFG(8, 4, 1024, 2, 6, 4, 2, "log4"),  // 44: as 27, 4 targets per thread
     NBGB_CFG(8, 2, 1024, 3, 6, 4, 2, "log4"),  // 45: as 27, 3 ring stages
+    NBGB_CFG(8, 2, 1024, 2, 7, 4, 2, "pf_log4"),  // 46: as 27, sources loaded a pair ahead
+    NBGB_CFG(8, 2, 2048, 2, 7, 4, 2, "pf_log4"),  // 47: as 46, 2048-body tiles
 };
 static const int kNumConfigs = (int)(sizeof(kConfigs) / sizeof(kConfigs[0]));
 // Relative throughput of each configuration (interactions/s per resident
@@ -565,7 +609,7 @@ static double g_speed[] = {
     0.990, 0.966, 0.873, 0.936, 0.987, 0.981, 0.981, 0.982, 0.981, 0.928,  // 10-19
     0.987, 0.951, 0.974, 0.900, 0.997, 1.000, 0.977, 1.057, 1.030, 1.026,  // 20-29
     1.034, 1.009, 1.016, 0.997, 1.020, 1.057, 1.000, 1.000, 1.000, 1.000,  // 30-39
-    1.000, 1.000, 1.000, 1.000, 1.000, 1.000,                              // 40-45
+    1.000, 1.000, 1.000, 1.000, 1.000, 1.000, 1.000, 1.000,                // 40-47
 };
 static_assert(sizeof(g_speed) / sizeof(g_speed[0]) == sizeof(kConfigs) / sizeof(kConfigs[0]),
               "one speed per configuration");
@@ -634,7 +678,7 @@ static void fill_layout(ForcePlan &pl, size_t n, size_t nt = 0) {
     pl.block_bodies = (int)bi;
     pl.tile_bodies = cf.jt;
     pl.js_vpb = cf.mode == 4 ? 2 : 1;
-    pl.js_log = cf.mode == 6 ? 1 : 0;
+    pl.js_log = (cf.mode == 6 || cf.mode == 7) ? 1 : 0;
     pl.nblocks = (int)(((nt ? nt : n) + bi - 1) / bi);
     pl.ntiles = (int)((n + cf.jt - 1) / cf.jt);
     pl.ni_pad = (size_t)pl.nblocks * bi;

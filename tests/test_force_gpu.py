@@ -71,8 +71,8 @@ def test_drop_in_entry_matches_reference(cuda, case):
     assert np.isfinite(nb.crosscheck_max_rel_error(out, g["force_aos"]))
 
 
-NUM_CONFIGS = 46
-LOG_DOMAIN_CONFIGS = range(27, 46)  # every fourth source pair in the log domain
+NUM_CONFIGS = 48
+LOG_DOMAIN_CONFIGS = range(27, 48)  # every fourth source pair in the log domain
 NEGATIVE_MASS = 0x8  # NBGB_STATUS_NEGATIVE_MASS
 
 
