@@ -609,11 +609,11 @@ static double g_speed[] = {
     0.990, 0.966, 0.873, 0.936, 0.987, 0.981, 0.981, 0.982, 0.981, 0.928,  // 10-19
     0.987, 0.951, 0.974, 0.900, 0.997, 1.000, 0.977, 1.057, 1.030, 1.026,  // 20-29
     1.034, 1.009, 1.016, 0.997, 1.020, 1.057, 1.000, 1.000, 1.000, 1.000,  // 30-39
-    1.000, 1.000, 1.000, 1.000, 1.000, 1.000, 1.000, 1.000,                // 40-47
+    1.000, 1.000, 1.000, 1.000, 1.000, 1.060, 1.000, 1.000,                // 40-47
 };
 static_assert(sizeof(g_speed) / sizeof(g_speed[0]) == sizeof(kConfigs) / sizeof(kConfigs[0]),
               "one speed per configuration");
-static const int kDefaultCandidates[] = {27, 28, 29, 30, 31, 32, 25, 24, 10, 20, 2, 3, 5};
+static const int kDefaultCandidates[] = {45, 27, 28, 29, 30, 31, 32, 25, 24, 10, 20, 2, 3, 5};
 // Candidates without log-domain pairs, for masses that have no logarithm
 // (negative masses).
 static const int kRsqrtCandidates[] = {25, 24, 10, 20, 2, 3, 5};
