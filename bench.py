@@ -19,9 +19,10 @@ interaction (src/nbody.cu:1027).
   roofline  the force kernel: 20 N^2 FLOP / its CUDA-event launch time, over
             the FP32 pipe peak measured by the library's FMA microbenchmark
             on this GPU (max of scalar and f32x2), plus the MUFU ceiling;
-            `integrate` holds the same for the two HBM-bound FP64 integrate
-            kernels (algorithmic bytes / CUDA-event time over the measured
-            copy bandwidth)
+            `integrate` holds the same for the HBM-bound integrate kernels:
+            the FP64 kick+drift and half kick of the resident loop and the
+            reference-mode step (algorithmic bytes / CUDA-event time over the
+            measured copy bandwidth)
   cpu_baseline  the oracle's restatement of the reference's CPU_SOA loop
             (OpenMP, all host threads) on a bounded sample of target bodies
             against all N sources
@@ -336,7 +337,8 @@ def run_gb300(args, ws, rank, local):
     cfg_name = nb.force_config_names()[cfg] if args.force == 'onesided' else 'newton3'
     traffic = profiled_traffic(cfg_name, n, nsplit)
     sysm.close()
-    integrate = integrate_roofline(n, kd_ms, hk_ms)
+    integrate = integrate_roofline(n, kd_ms, hk_ms,
+                                   reference_step_ms(n, dev, torch.cuda.current_stream(), flush))
 
     # e2e: the drop-in entry point with host buffers
     pm_h = torch.from_numpy(pm_np).pin_memory()
@@ -417,17 +419,44 @@ class L2Flush:
 # read and written once)
 KICK_DRIFT_BYTES = 148  # read x, v (48), a (16), m (4); write x, v (48), posMass, j-stream (32)
 HALF_KICK_BYTES = 64    # read v (24), a (16); write v (24)
+REFERENCE_STEP_BYTES = 80  # read posMass, velInvMass, force; write posMass, velInvMass
 
 
-def integrate_roofline(n, kd_ms, hk_ms):
-    """HBM roofline of the two FP64 integrate kernels from CUDA-event times,
-    each launched right after the L2 flush (cold state): the kick+drift of
-    every timed step, and the closing half kick, which runs only when the
-    velocities are read (timed three times after the steps)."""
+def reference_step_ms(n, dev, stream, flush, reps=5):
+    """CUDA-event times of the reference-mode integrate (integrateOne on the
+    GPU, nbgb_integrate_reference) on N bodies of device arrays, each launch
+    right after the L2 flush."""
+    import torch
+
+    import nbody_gb300 as nb
+    g = torch.Generator(device="cpu").manual_seed(3)
+    pm = torch.rand((n, 4), generator=g).to(dev)
+    vm = torch.rand((n, 4), generator=g).to(dev)
+    f = torch.rand((n, 4), generator=g).to(dev)
+    out = []
+    for _ in range(reps + 1):
+        with torch.cuda.stream(stream):
+            flush()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            nb.integrate_reference(pm, vm, f, 1e-6, 0.95, stream=stream.cuda_stream)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return out[1:]
+
+
+def integrate_roofline(n, kd_ms, hk_ms, ref_ms=()):
+    """HBM roofline of the integrate kernels from CUDA-event times, each
+    launched right after the L2 flush (cold state): the FP64 kick+drift of
+    every timed step, the closing half kick, which runs only when the
+    velocities are read (timed three times after the steps), and the
+    reference-mode step (integrateOne) on the same N."""
     peak, src = hbm_peak()
     out = {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": src}
     for name, per_body, ms in (("kick_drift", KICK_DRIFT_BYTES, kd_ms),
-                               ("half_kick", HALF_KICK_BYTES, hk_ms)):
+                               ("half_kick", HALF_KICK_BYTES, hk_ms),
+                               ("reference_step", REFERENCE_STEP_BYTES, ref_ms)):
         t = float(np.median(ms)) if ms else 0.0
         gbs = per_body * float(n) / (t * 1e-3) / 1e9 if t > 0 else None
         out[name] = {"bytes_per_body": per_body, "bytes": per_body * n, "ms": t,
