@@ -3,7 +3,7 @@
     python -m nbody_gb300 [--bodies N] [--iterations N] [--cycle-after N]
         [--seed N] [--no-crosscheck] [--no-cpu] [--gpus N] [--list]
         [--algorithm NAME|INDEX] [--graphics] [--verbose]
-        [--softening2 X] [--dt X] [--integrator reference|kdk64]
+        [--softening2 X] [--dt X] [--integrator reference|reference-fused|kdk64]
 
 Mirrors the reference driver's command line (src/nbody.cu:645-701, 749-916)
 and per-step line (src/nbody.cu:1024-1053), so tools that parse the
@@ -67,7 +67,11 @@ def parse(argv=None):
     ap.add_argument("--softening2", type=float, default=0.1 * 0.1)
     ap.add_argument("--dt", type=float, default=0.016)
     ap.add_argument("--damping", type=float, default=0.95)
-    ap.add_argument("--integrator", choices=["reference", "kdk64"], default="reference")
+    ap.add_argument("--integrator", choices=["reference", "reference-fused", "kdk64"],
+                    default="reference",
+                    help="reference: integrateOne, each operation rounded; reference-fused: "
+                         "the same with the position update fused, as the reference binary "
+                         "built with its own flags computes it; kdk64: FP64 leapfrog")
     return ap.parse_args(argv)
 
 
@@ -135,9 +139,11 @@ def main(argv=None) -> int:
     sys.stderr.write(msg + "\n")
 
     pm, vm = nb.ic_reference(n, a.seed)
-    integ = nb.INTEGRATOR_REFERENCE if a.integrator == "reference" else nb.INTEGRATOR_KDK64
+    integ = {"reference": nb.INTEGRATOR_REFERENCE,
+             "reference-fused": nb.INTEGRATOR_REFERENCE_FUSED,
+             "kdk64": nb.INTEGRATOR_KDK64}[a.integrator]
     s = nb.System(n, integ, a.softening2, a.dt, a.damping)
-    if integ == nb.INTEGRATOR_REFERENCE:
+    if integ != nb.INTEGRATOR_KDK64:
         s.set_state(pm, vm)
     else:
         s.set_state64(pm[:, :3].astype(np.float64), vm[:, :3].astype(np.float64),
