@@ -395,6 +395,10 @@ def run_gb300(args, ws, rank, local):
     if args.force == "onesided" and not args.no_newton3:
         line["newton3"] = measure_newton3(args, n, p3, v3, pm_np, dev, ffma, ffma2, fp32_peak,
                                           flush)
+    try:
+        line["reference_mode"] = reference_mode_steps(dev)
+    except Exception as e:  # a side measurement: keep the line
+        line["reference_mode"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         rate, el, info = cpu_rate(pm_np, args.cpu_seconds)
         line["cpu_baseline"] = dict(value=rate, unit=UNIT, **info)
@@ -444,6 +448,57 @@ def reference_step_ms(n, dev, stream, flush, reps=5):
         torch.cuda.synchronize()
         out.append(e0.elapsed_time(e1))
     return out[1:]
+
+
+def reference_mode_steps(dev, n=16384, steps=400):
+    """Milliseconds per reference-mode step on the plain N = 16,384 case
+    (uniform ball, eps2 = 1e-4, dt = 0.01, damping 0.95, contracted drift):
+    the System's resident loop, one launch per step (the integrate runs in
+    the force kernel's epilogue; graph-launched), against the two-launch form
+    (standalone force kernel, then integrateOne) captured in one CUDA graph
+    of the same steps.  Both on L2-resident state: this is the launch and
+    tail cost the fusion removes, not an HBM figure."""
+    import torch
+
+    import nbody_gb300 as nb
+    pm, vm = nb.ic_uniform_ball(n, 16384)
+    s = nb.System(n, nb.INTEGRATOR_REFERENCE_FUSED, 1e-4, 0.01, 0.95)
+    s.set_state(pm, vm)
+    st = torch.cuda.ExternalStream(s.stream, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.step(8)
+    s.synchronize()
+    e0.record(st)
+    s.step(steps)
+    e1.record(st)
+    s.synchronize()
+    fused_ms = e0.elapsed_time(e1) / steps
+    s.close()
+    tp = torch.from_numpy(pm).to(dev)
+    tv = torch.from_numpy(vm).to(dev)
+    f = torch.empty_like(tp)
+    ws = nb.Workspace()
+    side = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(side):
+        for _ in range(3):  # plans the workspace outside the capture
+            nb.force(tp, 1e-4, out=f, workspace=ws)
+            nb.integrate_reference(tp, tv, f, 0.01, 0.95, fused_drift=True)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        for _ in range(steps):
+            nb.force(tp, 1e-4, out=f, workspace=ws)
+            nb.integrate_reference(tp, tv, f, 0.01, 0.95, fused_drift=True)
+    g.replay()
+    torch.cuda.synchronize()
+    e0.record()
+    g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    two_ms = e0.elapsed_time(e1) / steps
+    return {"n_bodies": n, "steps": steps, "ms_per_step_one_launch": fused_ms,
+            "ms_per_step_two_launches": two_ms, "speedup": two_ms / fused_ms,
+            "state": "L2-resident (4 arrays x 256 KiB)"}
 
 
 def integrate_roofline(n, kd_ms, hk_ms, ref_ms=()):

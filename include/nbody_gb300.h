@@ -221,7 +221,10 @@ NBGB_API int nbgb_system_set_force_algorithm(nbgb_system *sys, int algorithm);
    the system's stream (steps then run eagerly); nbgb_system_last_force_ms
    reads the latest force launch, nbgb_system_last_integrate_ms the latest
    integrate launches: step_ms the reference integrate or the FP64
-   kick+drift, half_kick_ms the closing FP64 half kick (0 if none ran). */
+   kick+drift, half_kick_ms the closing FP64 half kick (0 if none ran).  With
+   a reference integrator and the one-sided kernel the integrate runs inside
+   the force launch (its epilogue), so the force time covers both and
+   nbgb_system_last_integrate_ms has nothing to report (-1). */
 NBGB_API int nbgb_system_set_timing(nbgb_system *sys, int enable);
 NBGB_API int nbgb_system_last_force_ms(nbgb_system *sys, float *ms);
 NBGB_API int nbgb_system_last_integrate_ms(nbgb_system *sys, float *step_ms,

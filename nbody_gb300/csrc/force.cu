@@ -70,6 +70,7 @@ struct ForceParams {
     int nfull;     // i-blocks 0..nfull-1 are whole units; the rest are split
     int ni_split;  // (nblocks - nfull) * BI
     float eps2;
+    FusedIntegrate fi;  // fi.vel == nullptr: forces only
 };
 
 // ---------------------------------------------------------------------------
@@ -113,6 +114,49 @@ __global__ void pack_jstream_dup_kernel(const float4 *__restrict__ pm, float4 *_
     }
     if (q < ncounters)
         counters[q] = 0u;
+}
+
+// The reference integrator (integrateOne, src/nbody.cu:158-182) applied to
+// target i by the unit that produced its final force F: v += (F invMass) dt;
+// v *= damping; x += v dt, each operation rounded separately or, fused drift,
+// x = fma(v, dt, x) -- the same arithmetic as integrate_reference_kernel, so
+// the results are identical.  Writes posMass (mass kept), velInvMass and body
+// i's entry of the next step's j-stream (fi.js, the other buffer: the current
+// one is still being read by other units).  Only the last unit of an
+// i-block writes its targets, after every unit of that i-block has loaded
+// them, so no unit reads a target this launch has moved.
+__device__ __forceinline__ void fused_integrate(const FusedIntegrate &fi, int i, float x, float y,
+                                                float z, float m, float fx, float fy, float fz) {
+    float4 v = fi.vel[i];
+    const float im = v.w, dt = fi.dt;
+    v.x = __fmul_rn(__fadd_rn(v.x, __fmul_rn(__fmul_rn(fx, im), dt)), fi.damping);
+    v.y = __fmul_rn(__fadd_rn(v.y, __fmul_rn(__fmul_rn(fy, im), dt)), fi.damping);
+    v.z = __fmul_rn(__fadd_rn(v.z, __fmul_rn(__fmul_rn(fz, im), dt)), fi.damping);
+    if (fi.fused_drift) {
+        x = __fmaf_rn(v.x, dt, x);
+        y = __fmaf_rn(v.y, dt, y);
+        z = __fmaf_rn(v.z, dt, z);
+    } else {
+        x = __fadd_rn(x, __fmul_rn(v.x, dt));
+        y = __fadd_rn(y, __fmul_rn(v.y, dt));
+        z = __fadd_rn(z, __fmul_rn(v.z, dt));
+    }
+    fi.pm[i] = make_float4(x, y, z, m);
+    fi.vel[i] = v;
+    const int q = i >> 1, h = i & 1;
+    float w = m;
+    if (fi.js_log && jstream_log_slot(q))
+        w = jstream_log_mass(w);
+    if (fi.js_vpb == 2) {
+        fi.js[2 * i] = make_float4(x, x, y, y);
+        fi.js[2 * i + 1] = make_float4(z, z, w, w);
+    } else {
+        float *a = reinterpret_cast<float *>(fi.js + 2 * q);
+        a[h] = x;
+        a[2 + h] = y;
+        a[4 + h] = z;
+        a[6 + h] = w;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -469,9 +513,12 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const int i = ib * BI + k * NT + tid;
-            if (i < p.n)
-                p.force[i] = make_float4(hx[k] + lx[k], hy[k] + ly[k], hz[k] + lz[k],
-                                         POT ? -((hp[k] - self[k]) + lp[k]) : 0.f);
+            if (i < p.n) {
+                const float fx = hx[k] + lx[k], fy = hy[k] + ly[k], fz = hz[k] + lz[k];
+                p.force[i] = make_float4(fx, fy, fz, POT ? -((hp[k] - self[k]) + lp[k]) : 0.f);
+                if (!POT && p.fi.vel)
+                    fused_integrate(p.fi, i, px[k], py[k], pz[k], pm_self[k], fx, fy, fz);
+            }
         }
         return;
     }
@@ -523,7 +570,10 @@ __global__ void __launch_bounds__(W * 32, MINB) force_kernel(ForceParams p) {
                 Lp += l.w;
             }
         }
-        p.force[i] = make_float4(Hx + Lx, Hy + Ly, Hz + Lz, POT ? -((Hp - self[k]) + Lp) : 0.f);
+        const float fx = Hx + Lx, fy = Hy + Ly, fz = Hz + Lz;
+        p.force[i] = make_float4(fx, fy, fz, POT ? -((Hp - self[k]) + Lp) : 0.f);
+        if (!POT && p.fi.vel)
+            fused_integrate(p.fi, i, px[k], py[k], pz[k], pm_self[k], fx, fy, fz);
     }
 }
 
@@ -839,7 +889,7 @@ int plan_force_within(size_t n, size_t max_bytes, ForcePlan &pl) {
 }
 
 int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,
-                 float eps2, void *workspace, cudaStream_t stream) {
+                 float eps2, void *workspace, cudaStream_t stream, const FusedIntegrate *fi) {
     const ForceConfig &cf = kConfigs[pl.config];
     char *ws = (char *)workspace;
     ForceParams p;
@@ -856,6 +906,15 @@ int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, cons
     p.nfull = pl.nfull;
     p.ni_split = split_blocks(pl) * pl.block_bodies;
     p.eps2 = eps2;
+    if (fi) {
+        if (!fi->vel || !fi->pm || !fi->js || pl.nt || cf.mode == 5)
+            return NBGB_ERR_INVALID_ARGUMENT;
+        p.fi = *fi;
+        p.fi.js_vpb = pl.js_vpb;
+        p.fi.js_log = pl.js_log;
+    } else {
+        p.fi = FusedIntegrate{};
+    }
     const size_t smem = (size_t)cf.stages * cf.jt * 16 * pl.js_vpb;
     void *args[] = {&p};
     const unsigned grid = (unsigned)plan_units(pl);
@@ -863,12 +922,13 @@ int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, cons
     return e == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
-int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream) {
+int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream,
+                float4 *js_out) {
     char *ws = (char *)workspace;
-    float4 *js = (float4 *)(ws + pl.off_js);
-    unsigned *cnt = split_blocks(pl) ? (unsigned *)(ws + pl.off_cnt) : nullptr;
+    float4 *js = js_out ? js_out : (float4 *)(ws + pl.off_js);
+    unsigned *cnt = (!js_out && split_blocks(pl)) ? (unsigned *)(ws + pl.off_cnt) : nullptr;
     const int npad = pl.ntiles * pl.tile_bodies;
-    const int ncnt = split_blocks(pl);
+    const int ncnt = cnt ? split_blocks(pl) : 0;
     const int work = std::max(npad / 2, ncnt);
     const int tb = 256;
     if (pl.js_vpb == 2)

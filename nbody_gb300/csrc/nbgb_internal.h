@@ -51,10 +51,27 @@ inline int split_blocks(const ForcePlan &pl) { return pl.nsplit > 1 ? pl.nblocks
 inline long long plan_units(const ForcePlan &pl) {
     return (long long)pl.nblocks + (long long)split_blocks(pl) * (pl.nsplit - 1);
 }
-int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream);
-// jstream == nullptr: use the j-stream inside the workspace.
+// js_out == nullptr: the j-stream inside the workspace (and the split
+// counters are zeroed); else only that j-stream buffer is written.
+int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cudaStream_t stream,
+                float4 *js_out = nullptr);
+// The reference integrator fused into the force launch's epilogue: pm is the
+// posMass the launch reads its targets from (updated in place), js the
+// j-stream buffer for the next step (not the one being read).  js_vpb and
+// js_log are taken from the plan.
+struct FusedIntegrate {
+    float4 *pm = nullptr;
+    float4 *vel = nullptr;
+    float4 *js = nullptr;
+    float dt = 0.f, damping = 1.f;
+    int fused_drift = 0;
+    int js_vpb = 1, js_log = 0;
+};
+// jstream == nullptr: use the j-stream inside the workspace.  fi != nullptr
+// (full systems only, not row slices): integrate every target after its force.
 int launch_force(const ForcePlan &pl, float4 *force, const float4 *posMass, const float4 *jstream,
-                 float eps2, void *workspace, cudaStream_t stream);
+                 float eps2, void *workspace, cudaStream_t stream,
+                 const FusedIntegrate *fi = nullptr);
 int read_and_clear_status(unsigned *bits);
 int read_status_ensemble(unsigned *bits);
 int read_status_integrate(unsigned *bits);

@@ -53,6 +53,14 @@ struct nbgb_system {
     bool v_lag = false;        // KDK: velocities trail by half a step (closing kick pending)
     bool use_graph = true;
     cudaGraphExec_t graph = nullptr;
+    // reference integrators: the force launch also integrates (fused
+    // epilogue) and writes the next step's j-stream into the other of two
+    // buffers (the workspace's and js2); js_cur names the one to read
+    float4 *js2 = nullptr;
+    size_t js2_bytes = 0;
+    bool js2_ready = false;  // js2 holds the plan's zero-mass padding
+    int js_cur = 0;
+    cudaGraphExec_t graph2 = nullptr;  // the step body starting from buffer 1
     // optional per-launch timing of the force kernel (bypasses the graph)
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -77,6 +85,16 @@ struct nbgb_system {
 namespace {
 
 float4 *js_of(nbgb_system *s) { return (float4 *)((char *)s->ws + s->plan.off_js); }
+float4 *js_cur_ptr(nbgb_system *s) { return s->js_cur ? s->js2 : js_of(s); }
+float4 *js_next_ptr(nbgb_system *s) { return s->js_cur ? js_of(s) : s->js2; }
+
+void drop_graphs(nbgb_system *s) {
+    if (s->graph)
+        cudaGraphExecDestroy(s->graph);
+    if (s->graph2)
+        cudaGraphExecDestroy(s->graph2);
+    s->graph = s->graph2 = nullptr;
+}
 unsigned *cnt_of(nbgb_system *s) {
     return nbgb::split_blocks(s->plan) ? (unsigned *)((char *)s->ws + s->plan.off_cnt) : nullptr;
 }
@@ -99,9 +117,34 @@ int mark(nbgb_system *s, int ev) {
 int ensure_jstream(nbgb_system *s) {
     if (s->js_valid)
         return NBGB_OK;
-    int rc = nbgb::launch_pack(s->plan, s->pm, s->ws, s->stream);
+    int rc = s->js_cur ? nbgb::launch_pack(s->plan, s->pm, s->ws, s->stream, s->js2)
+                       : nbgb::launch_pack(s->plan, s->pm, s->ws, s->stream);
     if (rc == NBGB_OK)
         s->js_valid = true;
+    return rc;
+}
+
+// Reference integrators: the second j-stream buffer, sized for the plan and
+// packed once so its zero-mass padding is in place (the fused integrate
+// writes the real bodies' entries every step).
+int ensure_js2(nbgb_system *s) {
+    const size_t bytes =
+        (size_t)s->plan.ntiles * s->plan.tile_bodies * 16 * (size_t)s->plan.js_vpb;
+    if (s->js2_ready && s->js2_bytes == bytes)
+        return NBGB_OK;
+    if (s->js2_bytes != bytes) {
+        cudaFree(s->js2);
+        s->js2 = nullptr;
+        s->js2_bytes = 0;
+        if (cudaMalloc(&s->js2, bytes) != cudaSuccess) {
+            s->js2 = nullptr;
+            return NBGB_ERR_NO_MEMORY;
+        }
+        s->js2_bytes = bytes;
+    }
+    int rc = nbgb::launch_pack(s->plan, s->pm, s->ws, s->stream, s->js2);
+    if (rc == NBGB_OK)
+        s->js2_ready = true;
     return rc;
 }
 
@@ -112,18 +155,19 @@ int force_pass(nbgb_system *s) {
     int rc = ensure_jstream(s);
     if (rc != NBGB_OK)
         return rc;
-    return nbgb::launch_force(s->plan, s->force, s->pm, js_of(s), s->eps2, s->ws, s->stream);
+    return nbgb::launch_force(s->plan, s->force, s->pm, js_cur_ptr(s), s->eps2, s->ws, s->stream);
 }
 
-// The force launch of a step, bracketed by events when timing is on.
-int timed_force(nbgb_system *s) {
+// The force launch of a step, bracketed by events when timing is on; fi:
+// the reference integrator fused into it (one-sided kernel only).
+int timed_force(nbgb_system *s, const nbgb::FusedIntegrate *fi = nullptr) {
     if (s->timing && cudaEventRecord(s->ev0, s->stream) != cudaSuccess)
         return NBGB_ERR_CUDA;
     int rc = s->algorithm == 1
                  ? nbgb_force_newton3((float *)s->force, (const float *)s->pm, s->eps2, s->n,
                                       s->ws_n3, s->ws_n3_bytes, s->stream)
-                 : nbgb::launch_force(s->plan, s->force, s->pm, js_of(s), s->eps2, s->ws,
-                                      s->stream);
+                 : nbgb::launch_force(s->plan, s->force, s->pm, js_cur_ptr(s), s->eps2, s->ws,
+                                      s->stream, fi);
     if (rc == NBGB_OK && s->timing) {
         if (cudaEventRecord(s->ev1, s->stream) != cudaSuccess)
             return NBGB_ERR_CUDA;
@@ -133,15 +177,32 @@ int timed_force(nbgb_system *s) {
 }
 
 // One reference step: force(x) then integrate (writes x' and its j-stream).
+// With the one-sided kernel both happen in one launch: the force kernel's
+// epilogue integrates each body once its force is final and writes the next
+// step's j-stream into the other buffer, which then becomes current.  With
+// the Newton-3 kernel the integrate is its own launch.
 int ref_step_body(nbgb_system *s) {
+    const int fused_drift = s->integrator == NBGB_INTEGRATOR_REFERENCE_FUSED ? 1 : 0;
+    if (s->algorithm == 0) {
+        nbgb::FusedIntegrate fi;
+        fi.pm = s->pm;
+        fi.vel = s->vel;
+        fi.js = js_next_ptr(s);
+        fi.dt = s->dt;
+        fi.damping = s->damping;
+        fi.fused_drift = fused_drift;
+        int rc = timed_force(s, &fi);
+        if (rc == NBGB_OK)
+            s->js_cur ^= 1;
+        return rc;
+    }
     int rc = timed_force(s);
     if (rc == NBGB_OK)
         rc = mark(s, 0);
     if (rc == NBGB_OK)
         rc = nbgb::launch_integrate_reference(
-            s->pm, s->vel, s->force, s->dt, s->damping, s->n,
-            s->integrator == NBGB_INTEGRATOR_REFERENCE_FUSED ? 1 : 0, js_of(s), s->plan.js_vpb,
-            s->plan.js_log, npad_of(s), cnt_of(s), ncnt_of(s), s->stream);
+            s->pm, s->vel, s->force, s->dt, s->damping, s->n, fused_drift, js_cur_ptr(s),
+            s->plan.js_vpb, s->plan.js_log, npad_of(s), cnt_of(s), ncnt_of(s), s->stream);
     if (rc == NBGB_OK && (rc = mark(s, 1)) == NBGB_OK && s->timing)
         s->itimed = true;
     return rc;
@@ -213,11 +274,10 @@ int fit_plan_to_masses(nbgb_system *s, const float *m, size_t stride) {
     // split counters start at zero
     if (cudaMemsetAsync(s->ws, 0, s->ws_bytes, s->stream) != cudaSuccess)
         return NBGB_ERR_CUDA;
-    if (s->graph) {
-        cudaGraphExecDestroy(s->graph);
-        s->graph = nullptr;
-    }
+    drop_graphs(s);
     s->plan = pl;
+    s->js2_ready = false;  // repacked (and resized) for the new plan
+    s->js_cur = 0;
     return NBGB_OK;
 }
 
@@ -229,8 +289,7 @@ int check_device_status() {
 }
 
 void free_all(nbgb_system *s) {
-    if (s->graph)
-        cudaGraphExecDestroy(s->graph);
+    drop_graphs(s);
     if (s->ev0)
         cudaEventDestroy(s->ev0);
     if (s->ev1)
@@ -244,6 +303,7 @@ void free_all(nbgb_system *s) {
     cudaFree(s->x64);
     cudaFree(s->mass);
     cudaFree(s->ws);
+    cudaFree(s->js2);
     cudaFree(s->diag_ws);
     cudaFree(s->ws_n3);
     cudaFree(s->phi);
@@ -253,11 +313,15 @@ void free_all(nbgb_system *s) {
         cudaStreamDestroy(s->stream);
 }
 
+// The reference step with the integrate fused into the force launch, which
+// alternates between the two j-stream buffers.
+bool alternates(const nbgb_system *s) {
+    return reference_integrator(s->integrator) && s->algorithm == 0;
+}
+
 // Capture one step body into a graph (reference: force+integrate; KDK: full
 // kick + drift + force).
-int build_graph(nbgb_system *s) {
-    if (s->graph)
-        return NBGB_OK;
+int capture_step(nbgb_system *s, cudaGraphExec_t *out) {
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return NBGB_ERR_CUDA;
@@ -268,9 +332,32 @@ int build_graph(nbgb_system *s) {
             cudaGraphDestroy(g);
         return NBGB_ERR_CUDA;
     }
-    e = cudaGraphInstantiate(&s->graph, g, 0);
+    e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     return e == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
+}
+
+// An alternating step needs one graph per starting buffer: graph reads
+// buffer 0 and writes buffer 1, graph2 the reverse.
+int build_graph(nbgb_system *s) {
+    if (s->graph)
+        return NBGB_OK;
+    if (!alternates(s))
+        return capture_step(s, &s->graph);
+    const int cur = s->js_cur;
+    s->js_cur = 0;
+    int rc = capture_step(s, &s->graph);
+    s->js_cur = 1;
+    if (rc == NBGB_OK)
+        rc = capture_step(s, &s->graph2);
+    s->js_cur = cur;  // capturing toggled it
+    if (rc != NBGB_OK)
+        drop_graphs(s);
+    return rc;
+}
+
+cudaGraphExec_t step_graph(nbgb_system *s) {
+    return alternates(s) && s->js_cur ? s->graph2 : s->graph;
 }
 
 }  // namespace
@@ -413,7 +500,9 @@ NBGB_API int nbgb_system_step(nbgb_system *s, int nsteps) {
         return NBGB_ERR_INVALID_ARGUMENT;
     if (nsteps == 0)
         return NBGB_OK;
-    int rc = ensure_jstream(s);
+    int rc = alternates(s) ? ensure_js2(s) : NBGB_OK;
+    if (rc == NBGB_OK)
+        rc = ensure_jstream(s);
     if (rc != NBGB_OK)
         return rc;
     const bool graph = s->use_graph && !s->timing;
@@ -422,8 +511,10 @@ NBGB_API int nbgb_system_step(nbgb_system *s, int nsteps) {
             return rc;
         for (int k = 0; k < nsteps; k++) {
             if (graph) {
-                if (cudaGraphLaunch(s->graph, s->stream) != cudaSuccess)
+                if (cudaGraphLaunch(step_graph(s), s->stream) != cudaSuccess)
                     return NBGB_ERR_CUDA;
+                if (alternates(s))
+                    s->js_cur ^= 1;
             } else if ((rc = ref_step_body(s)) != NBGB_OK) {
                 return rc;
             }
@@ -480,10 +571,7 @@ NBGB_API int nbgb_system_set_force_algorithm(nbgb_system *s, int algorithm) {
     int rc = sync_velocities(s);
     if (rc != NBGB_OK)
         return rc;
-    if (s->graph) {
-        cudaGraphExecDestroy(s->graph);
-        s->graph = nullptr;
-    }
+    drop_graphs(s);
     s->algorithm = algorithm;
     s->accel_valid = false;
     return NBGB_OK;
@@ -509,7 +597,9 @@ NBGB_API int nbgb_system_set_timing(nbgb_system *s, int enable) {
 
 // Milliseconds of the most recent timed integrate launches (waits for them):
 // step_ms the reference integrate or the FP64 kick+drift, half_kick_ms the
-// closing FP64 half kick (0 when none ran, e.g. reference integrators).
+// closing FP64 half kick (0 when none ran, e.g. reference integrators).  A
+// reference step on the one-sided kernel integrates inside the force launch
+// and times no separate integrate.
 NBGB_API int nbgb_system_last_integrate_ms(nbgb_system *s, float *step_ms, float *half_kick_ms) {
     if (!s || !s->timing || !s->itimed)
         return NBGB_ERR_INVALID_ARGUMENT;

@@ -154,4 +154,82 @@ def test_negative_masses_replan_the_system(cuda):
     f = sysm.get_force()
     ref = O.ieee().forces_aos(p_before, 1e-4)
     assert O.per_body_rel_error(f, ref)[0] <= TOL_FORCE
+    # the replanned system keeps stepping through both j-stream buffers
+    for _ in range(3):
+        p_before, v_before = sysm.get_state()
+        sysm.step(1)
+        f = sysm.get_force()
+        assert O.per_body_rel_error(f, O.ieee().forces_aos(p_before, 1e-4))[0] <= TOL_FORCE
+        O.ieee().integrate(p_before, v_before, f, 0.01, 0.95)
+        p_after, v_after = sysm.get_state()
+        assert np.array_equal(p_after, p_before) and np.array_equal(v_after, v_before)
     sysm.close()
+
+
+def _host_steps(p, v, m, fused, fn):
+    """m reference steps on host copies: forces by fn(p) on the GPU, then the
+    oracle's integrator (separately rounded or contracted drift)."""
+    import torch
+    f = None
+    for _ in range(m):
+        f = fn(torch.from_numpy(p).cuda()).cpu().numpy()
+        (O.ieee().integrate_contracted if fused else O.ieee().integrate)(p, v, f, 0.016, 0.95)
+    return f
+
+
+@pytest.mark.parametrize("n,integrator", [(1000, nb.INTEGRATOR_REFERENCE),
+                                          (10007, nb.INTEGRATOR_REFERENCE_FUSED),
+                                          (65536, nb.INTEGRATOR_REFERENCE),
+                                          (155677, nb.INTEGRATOR_REFERENCE_FUSED)])
+def test_fused_epilogue_step_is_force_then_integrate(cuda, n, integrator):
+    """A reference step on the one-sided kernel is one launch: the force
+    kernel's epilogue integrates each body once its force is final and writes
+    the next step's j-stream into the other of two buffers.  Every step must
+    equal the standalone force kernel on that step's positions followed by the
+    reference integrator, bit for bit: through graph launches (two graphs,
+    one per starting buffer), eager and timed steps, a state reset between
+    steps, and a detour through the Newton-3 algorithm (whose separate
+    integrate writes the current buffer)."""
+    fused = integrator == nb.INTEGRATOR_REFERENCE_FUSED
+    pm0, vm0 = nb.ic_reference(n, 11)
+    s = nb.System(n, integrator, 0.01, 0.016, 0.95)
+    assert s.plan() == nb.force_plan(n)[:2]  # same plan as the standalone force()
+    s.set_state(pm0, vm0)
+    p, v = pm0.copy(), vm0.copy()
+
+    def onesided(t):
+        return nb.force(t, 0.01)
+
+    def run(m, fn=onesided):
+        f = _host_steps(p, v, m, fused, fn)
+        s.step(m)
+        ps, vs = s.get_state()
+        assert np.array_equal(ps, p) and np.array_equal(vs, v), m
+        assert np.array_equal(s.get_force()[:, :3], f[:, :3]), m
+
+    for m in (1, 1, 3, 2):  # graph launches from either buffer, odd and even counts
+        run(m)
+    s.use_graph(False)
+    run(3)
+    s.set_timing(True)
+    run(1)
+    assert s.last_force_ms() > 0.0
+    with pytest.raises(nb.NbgbError):
+        s.last_integrate_ms()  # the integrate ran inside the force launch
+    s.set_timing(False)
+    s.use_graph(True)
+    pm1, vm1 = nb.ic_reference(n, 12)  # reset with the other buffer current
+    s.set_state(pm1, vm1)
+    p[:], v[:] = pm1, vm1
+    run(2)
+    run(1)
+    s.set_force_algorithm("newton3")
+    for _ in range(2):
+        s.step(1)
+        f = s.get_force()
+        (O.ieee().integrate_contracted if fused else O.ieee().integrate)(p, v, f, 0.016, 0.95)
+        ps, vs = s.get_state()
+        assert np.array_equal(ps, p) and np.array_equal(vs, v)
+    s.set_force_algorithm("onesided")
+    run(3)
+    s.close()
