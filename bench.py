@@ -396,7 +396,7 @@ def run_gb300(args, ws, rank, local):
         line["newton3"] = measure_newton3(args, n, p3, v3, pm_np, dev, ffma, ffma2, fp32_peak,
                                           flush)
     try:
-        line["reference_mode"] = reference_mode_steps(dev)
+        line["reference_mode"] = [reference_mode_steps(dev, m) for m in (1024, 4096, 16384)]
     except Exception as e:  # a side measurement: keep the line
         line["reference_mode"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -450,14 +450,14 @@ def reference_step_ms(n, dev, stream, flush, reps=5):
     return out[1:]
 
 
-def reference_mode_steps(dev, n=16384, steps=400):
-    """Milliseconds per reference-mode step on the plain N = 16,384 case
+def reference_mode_steps(dev, n=16384, steps=400):  # steps: a multiple of 8
+    """Milliseconds per reference-mode step on the plain case at N bodies
     (uniform ball, eps2 = 1e-4, dt = 0.01, damping 0.95, contracted drift):
     the System's resident loop, one launch per step (the integrate runs in
     the force kernel's epilogue; graph-launched), against the two-launch form
-    (standalone force kernel, then integrateOne) captured in one CUDA graph
-    of the same steps.  Both on L2-resident state: this is the launch and
-    tail cost the fusion removes, not an HBM figure."""
+    (standalone force kernel, then integrateOne), both replaying CUDA graphs
+    of 8 steps.  L2-resident state: this is the launch and tail cost the
+    fusion removes, not an HBM figure."""
     import torch
 
     import nbody_gb300 as nb
@@ -486,19 +486,20 @@ def reference_mode_steps(dev, n=16384, steps=400):
     torch.cuda.synchronize()
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g, stream=side):
-        for _ in range(steps):
+        for _ in range(8):
             nb.force(tp, 1e-4, out=f, workspace=ws)
             nb.integrate_reference(tp, tv, f, 0.01, 0.95, fused_drift=True)
     g.replay()
     torch.cuda.synchronize()
     e0.record()
-    g.replay()
+    for _ in range(steps // 8):
+        g.replay()
     e1.record()
     torch.cuda.synchronize()
     two_ms = e0.elapsed_time(e1) / steps
     return {"n_bodies": n, "steps": steps, "ms_per_step_one_launch": fused_ms,
             "ms_per_step_two_launches": two_ms, "speedup": two_ms / fused_ms,
-            "state": "L2-resident (4 arrays x 256 KiB)"}
+            "state": f"L2-resident (4 arrays x {n * 16 // 1024} KiB)"}
 
 
 def integrate_roofline(n, kd_ms, hk_ms, ref_ms=()):

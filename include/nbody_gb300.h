@@ -207,10 +207,13 @@ NBGB_API int nbgb_system_set_state(nbgb_system *sys, const float *posMass,
 /* KDK only: HOST double[N][3] positions and velocities, float[N] masses. */
 NBGB_API int nbgb_system_set_state64(nbgb_system *sys, const double *pos3, const double *vel3,
                                      const float *mass);
-/* Advance nsteps (asynchronous; steps replay one CUDA graph).  KDK: each
-   step is one kick+drift launch and one force launch; the call's closing
-   half kick is applied when the velocities are next read (getters,
-   diagnostics) or merged into the next call's opening kick. */
+/* Advance nsteps (asynchronous; whole groups of 8 steps replay a captured
+   CUDA graph, the rest launch directly).  Reference integrators with the
+   one-sided kernel: each step is one launch (the force kernel integrates
+   each body in its epilogue).  KDK: each step is one kick+drift launch and
+   one force launch; the call's closing half kick is applied when the
+   velocities are next read (getters, diagnostics) or merged into the next
+   call's opening kick. */
 NBGB_API int nbgb_system_step(nbgb_system *sys, int nsteps);
 /* KDK: apply a pending closing half kick now (asynchronous). */
 NBGB_API int nbgb_system_sync_velocities(nbgb_system *sys);

@@ -226,8 +226,10 @@ def last_status() -> int:
 # Device-resident simulation
 # ---------------------------------------------------------------------------
 class System:
-    """State resident in HBM; step() = force + integrate per step (one CUDA
-    graph per step body), no host round trip."""
+    """State resident in HBM; step() = force + integrate per step (reference
+    integrators on the one-sided kernel: one launch, the integrate in the
+    force kernel's epilogue; groups of 8 steps replay a CUDA graph), no host
+    round trip."""
 
     def __init__(self, N: int, integrator: int = INTEGRATOR_REFERENCE,
                  softeningSquared: float = 1e-4, dt: float = 0.01, damping: float = 1.0):

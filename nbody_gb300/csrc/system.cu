@@ -319,13 +319,22 @@ bool alternates(const nbgb_system *s) {
     return reference_integrator(s->integrator) && s->algorithm == 0;
 }
 
-// Capture one step body into a graph (reference: force+integrate; KDK: full
-// kick + drift + force).
+// Steps per captured graph.  Kernels inside one graph start back to back;
+// a graph holding one step (one or two kernels) launches no faster than the
+// kernels themselves.  Even, so that an alternating sequence ends on the
+// j-stream buffer it started from.
+constexpr int kGraphSteps = 8;
+
+// Capture kGraphSteps step bodies into one graph (reference: force with the
+// fused integrate, or force then integrate; KDK: full kick + drift + force).
 int capture_step(nbgb_system *s, cudaGraphExec_t *out) {
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return NBGB_ERR_CUDA;
-    int rc = reference_integrator(s->integrator) ? ref_step_body(s) : kdk_body(s, (double)s->dt);
+    int rc = NBGB_OK;
+    for (int k = 0; k < kGraphSteps && rc == NBGB_OK; k++)
+        rc = reference_integrator(s->integrator) ? ref_step_body(s)
+                                                 : kdk_body(s, (double)s->dt);
     cudaError_t e = cudaStreamEndCapture(s->stream, &g);
     if (rc != NBGB_OK || e != cudaSuccess) {
         if (g)
@@ -337,8 +346,8 @@ int capture_step(nbgb_system *s, cudaGraphExec_t *out) {
     return e == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 
-// An alternating step needs one graph per starting buffer: graph reads
-// buffer 0 and writes buffer 1, graph2 the reverse.
+// An alternating step sequence needs one graph per starting buffer: graph
+// starts by reading buffer 0, graph2 buffer 1.
 int build_graph(nbgb_system *s) {
     if (s->graph)
         return NBGB_OK;
@@ -350,7 +359,7 @@ int build_graph(nbgb_system *s) {
     s->js_cur = 1;
     if (rc == NBGB_OK)
         rc = capture_step(s, &s->graph2);
-    s->js_cur = cur;  // capturing toggled it
+    s->js_cur = cur;  // capturing toggled it (an even number of times)
     if (rc != NBGB_OK)
         drop_graphs(s);
     return rc;
@@ -505,20 +514,20 @@ NBGB_API int nbgb_system_step(nbgb_system *s, int nsteps) {
         rc = ensure_jstream(s);
     if (rc != NBGB_OK)
         return rc;
+    // whole graphs of kGraphSteps steps, the rest launched directly
     const bool graph = s->use_graph && !s->timing;
     if (reference_integrator(s->integrator)) {
-        if (graph && (rc = build_graph(s)) != NBGB_OK)
-            return rc;
-        for (int k = 0; k < nsteps; k++) {
-            if (graph) {
+        int k = 0;
+        if (graph && nsteps >= kGraphSteps) {
+            if ((rc = build_graph(s)) != NBGB_OK)
+                return rc;
+            for (; k + kGraphSteps <= nsteps; k += kGraphSteps)
                 if (cudaGraphLaunch(step_graph(s), s->stream) != cudaSuccess)
                     return NBGB_ERR_CUDA;
-                if (alternates(s))
-                    s->js_cur ^= 1;
-            } else if ((rc = ref_step_body(s)) != NBGB_OK) {
-                return rc;
-            }
         }
+        for (; k < nsteps; k++)
+            if ((rc = ref_step_body(s)) != NBGB_OK)
+                return rc;
         return NBGB_OK;
     }
     // KDK: the opening kick is a half kick when the velocities are in step
@@ -534,16 +543,17 @@ NBGB_API int nbgb_system_step(nbgb_system *s, int nsteps) {
     if ((rc = kdk_body(s, first)) != NBGB_OK)  // opening kick + drift + force
         return rc;
     s->v_lag = true;
-    if (nsteps > 1 && graph && (rc = build_graph(s)) != NBGB_OK)
-        return rc;
-    for (int k = 1; k < nsteps; k++) {
-        if (graph) {
+    int k = 1;
+    if (graph && nsteps - 1 >= kGraphSteps) {
+        if ((rc = build_graph(s)) != NBGB_OK)
+            return rc;
+        for (; k + kGraphSteps <= nsteps; k += kGraphSteps)
             if (cudaGraphLaunch(s->graph, s->stream) != cudaSuccess)
                 return NBGB_ERR_CUDA;
-        } else if ((rc = kdk_body(s, (double)s->dt)) != NBGB_OK) {
-            return rc;
-        }
     }
+    for (; k < nsteps; k++)
+        if ((rc = kdk_body(s, (double)s->dt)) != NBGB_OK)
+            return rc;
     return NBGB_OK;
 }
 

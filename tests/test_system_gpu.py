@@ -104,8 +104,23 @@ def test_graph_and_eager_steps_identical(cuda):
         s = nb.System(4096, nb.INTEGRATOR_REFERENCE, 0.01, 0.016, 0.95)
         s.use_graph(graph)
         s.set_state(pm0, vm0)
-        s.step(7)
+        s.step(19)  # two 8-step graphs and three direct steps
         out.append(s.get_state())
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_kdk64_graph_and_eager_steps_identical(cuda):
+    n = 3000
+    p, v, pm, _ = nb.ic_plummer(n, 5)
+    out = []
+    for graph in (True, False):
+        s = nb.System(n, nb.INTEGRATOR_KDK64, 1e-4, 0.002, 1.0)
+        s.use_graph(graph)
+        s.set_state64(p, v, pm[:, 3].copy())
+        s.step(20)  # an opening step, two 8-step graphs, three direct steps
+        s.step(9)   # a merged opening kick, one graph
+        out.append(s.get_state64())
         s.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
 
@@ -207,7 +222,7 @@ def test_fused_epilogue_step_is_force_then_integrate(cuda, n, integrator):
         assert np.array_equal(ps, p) and np.array_equal(vs, v), m
         assert np.array_equal(s.get_force()[:, :3], f[:, :3]), m
 
-    for m in (1, 1, 3, 2):  # graph launches from either buffer, odd and even counts
+    for m in (1, 8, 1, 9, 16, 2):  # 8-step graphs from either buffer, direct steps
         run(m)
     s.use_graph(False)
     run(3)
@@ -221,8 +236,8 @@ def test_fused_epilogue_step_is_force_then_integrate(cuda, n, integrator):
     pm1, vm1 = nb.ic_reference(n, 12)  # reset with the other buffer current
     s.set_state(pm1, vm1)
     p[:], v[:] = pm1, vm1
-    run(2)
     run(1)
+    run(8)
     s.set_force_algorithm("newton3")
     for _ in range(2):
         s.step(1)
@@ -230,6 +245,9 @@ def test_fused_epilogue_step_is_force_then_integrate(cuda, n, integrator):
         (O.ieee().integrate_contracted if fused else O.ieee().integrate)(p, v, f, 0.016, 0.95)
         ps, vs = s.get_state()
         assert np.array_equal(ps, p) and np.array_equal(vs, v)
+    s.step(8)  # a Newton-3 graph
+    p, v = s.get_state()
     s.set_force_algorithm("onesided")
     run(3)
+    run(8)
     s.close()
