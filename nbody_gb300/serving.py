@@ -382,12 +382,15 @@ def serve_study(n_req: int = 20000, rates=(10.0,), seed: int = 5, n_lo: int = 25
                 eps2: float = 1e-4, budget_gb: float = 120.0, slots: int = 512,
                 plain_sample: int | None = None, work_budgets=(2e10,), sub_work: float = 0.0,
                 records_out=None, express_n: int = 8192, express_ctas: int = 32,
-                newton3_min: int = 16384) -> dict:
+                newton3_min: int = 16384, plain_only: bool = False) -> dict:
     """Both servers on the same stream at each arrival rate.  The plain
     server's per-request service times are measured once (they do not depend
     on the arrival times) and replayed through the FIFO rule at every rate.
     The batched server runs once per work budget (interactions per tick
-    above which large requests wait); the first budget is the headline."""
+    above which large requests wait); the first budget is the headline.
+    plain_only: the plain server alone (re-measuring it after a change to
+    the single-system path; the batched server's results do not depend on
+    that path)."""
     base = make_requests(n_req, 1.0, seed, n_lo, n_hi, steps_lo, steps_hi)
     rng = np.random.default_rng(seed + 17)
     if plain_sample is None or plain_sample >= n_req:
@@ -416,15 +419,19 @@ def serve_study(n_req: int = 20000, rates=(10.0,), seed: int = 5, n_lo: int = 25
            "by_rate": []}
     for rate in rates:
         reqs = make_requests(n_req, rate, seed, n_lo, n_hi, steps_lo, steps_hi)
-        runs = [_batched_run(reqs, eps2, dt, budget_gb, slots, wb, sub_work, records_out,
-                             express_n, express_ctas, newton3_min) for wb in work_budgets]
-        b = runs[0]
+        runs = [] if plain_only else [
+            _batched_run(reqs, eps2, dt, budget_gb, slots, wb, sub_work, records_out,
+                         express_n, express_ctas, newton3_min) for wb in work_budgets]
         arrivals = [r["arrival"] for r in reqs]
         pfin = fifo_finish_times(arrivals, service)
         plat = [f - a for f, a in zip(pfin, arrivals)]
         pspan = pfin[-1] - arrivals[0]
         p = {"systems_per_s": n_req / pspan, "latency_p50_s": _pct(plat, 50),
              "latency_p99_s": _pct(plat, 99), "latency_mean_s": float(np.mean(plat))}
+        if plain_only:
+            out["by_rate"].append({"rate_per_s": rate, "plain": p})
+            continue
+        b = runs[0]
         row = {"rate_per_s": rate, "batched": b, "plain": p,
                "speedup_systems_per_s": b["systems_per_s"] / p["systems_per_s"]}
         if len(runs) > 1:
@@ -460,6 +467,8 @@ def main(argv=None):
                     help="CTA slots of the express lane's persistent force launch")
     ap.add_argument("--newton3-min", type=int, default=16384,
                     help="main-lane requests with N >= this use the Newton-3 kernel (0: none)")
+    ap.add_argument("--plain-only", action="store_true",
+                    help="measure and replay the plain server alone")
     ap.add_argument("--records", default=None,
                     help="write every batched request's record (JSON) to this path")
     a = ap.parse_args(argv)
@@ -468,7 +477,7 @@ def main(argv=None):
     recs = [] if a.records else None
     r = serve_study(a.requests, rates, a.seed, a.n_lo, a.n_hi, a.steps_lo, a.steps_hi, a.dt,
                     a.eps2, a.budget_gb, a.slots, a.plain_sample, budgets, a.sub_work, recs,
-                    a.express_n, a.express_ctas, a.newton3_min)
+                    a.express_n, a.express_ctas, a.newton3_min, a.plain_only)
     if a.records:
         with open(a.records, "w") as f:
             json.dump(recs, f)
