@@ -750,19 +750,70 @@ static void fill_layout(ForcePlan &pl, size_t n, size_t nt = 0) {
     pl.workspace_bytes = o;
 }
 
-// Cost model: units run in waves of (SMs x resident CTAs); a unit's time is
-// proportional to its tiles x JT x BI x (resident CTAs per SM) (plus a small
-// per-unit overhead), i.e. the SM's interaction throughput is taken as equal
-// across configurations, scaled by their measured relative speed.  For each
-// configuration and slice count s > 1 two decompositions are costed: every
-// i-block split s ways, and only the i-blocks left over after whole waves of
-// whole i-blocks split (nfull = whole waves x slots).  Of the plans within
-// 0.2 % of the cheapest, the one with the smallest workspace wins: the
-// tail-only split with few slices, whose partial sums stay in L2.
-static double unit_time(const ForceConfig &cf, int occ, long long ntl, int s, double speed) {
+// Cost model, fitted to graph-timed sweeps of the log-domain configurations
+// x slice counts at N = 2,048-262,144 on GB300 (it picks a plan within 3.5 %
+// of the fastest measured one at every size; the earlier wave-count model
+// was up to 42 % off below N = 131,072).  Time is counted in interactions one
+// SM evaluates at full occupancy, scaled by the configuration's measured
+// relative speed.  Units are dealt to the SMs in rounds of `occ` co-resident
+// CTAs and a round lasts as long as its busiest SM: a full round runs occ
+// units at the SM's full throughput, a last partial round k units at the
+// throughput k resident CTAs reach, share(k) = (1 - e^{-kW/tau}) /
+// (1 - e^{-occ W/tau}) with W warps per CTA and tau = 1.8 warps (eight warps
+// nearly saturate the pipes, four do not).  Every round also pays a fixed
+// latency (the first j-tile's copy, the epilogue), every unit a small
+// overhead, and a split i-block's combining unit reads one partial per
+// slice.  For each configuration and slice count s > 1 two decompositions
+// are costed: every i-block split s ways, and only the i-blocks left over
+// after whole rounds of whole i-blocks split (nfull = whole rounds x slots).
+// Of the plans within 0.2 % of the cheapest, the one with the smallest
+// workspace wins (fewest partial sums, which then stay in L2).
+constexpr double kUnitOverhead = 9.0;      // sources per unit and target
+constexpr double kCombinePerSlice = 37.0;  // sources per slice and target, combining unit
+constexpr double kRoundLatency = 29800.0;  // about 1.5 us of one SM's interactions
+constexpr double kWarpTau = 1.8;
+
+static double sm_share(int k, int warps, int occ) {
+    return (1.0 - std::exp(-(double)k * warps / kWarpTau)) /
+           (1.0 - std::exp(-(double)occ * warps / kWarpTau));
+}
+
+// `units` equal units of `sources` sources x bi targets; *k_last: resident
+// units per SM in the last round.
+static double rounds_time(long long units, double sources, double bi, int sms, int occ,
+                          int warps, double speed, int *k_last) {
+    const long long slots = (long long)sms * occ;
+    const double w = bi * (sources + kUnitOverhead) / speed;
+    const long long full = units / slots, r = units % slots;
+    double t = (double)full * (occ * w + kRoundLatency);
+    *k_last = occ;
+    if (r) {
+        const int k = (int)((r + sms - 1) / sms);
+        t += k * w / sm_share(k, warps, occ) + kRoundLatency;
+        *k_last = k;
+    }
+    return t;
+}
+
+// nfull whole i-blocks, then the remaining nb - nfull i-blocks split s ways.
+static double plan_cost(const ForceConfig &cf, int occ, int sms, long long nb, long long ntl,
+                        int s, long long nfull, double speed) {
     const double bi = (double)cf.warps * 32 * cf.k;
-    return (std::ceil((double)ntl / s) * cf.jt + 64.0 + (s > 1 ? 32.0 * s : 0.0)) * bi * occ /
-           speed;
+    double t = 0.0;
+    int k_last = occ;
+    if (nfull > 0)
+        t += rounds_time(nfull, (double)ntl * cf.jt, bi, sms, occ, cf.warps, speed, &k_last);
+    if (nb > nfull) {
+        if (s == 1) {
+            t += rounds_time(nb - nfull, (double)ntl * cf.jt, bi, sms, occ, cf.warps, speed,
+                             &k_last);
+        } else {
+            t += rounds_time((nb - nfull) * s, std::ceil((double)ntl / s) * cf.jt, bi, sms, occ,
+                             cf.warps, speed, &k_last);
+            t += s * kCombinePerSlice * bi / (speed * sm_share(k_last, cf.warps, occ));
+        }
+    }
+    return t;
 }
 
 // Enumerates the candidate decompositions of n sources / nt targets over
@@ -793,24 +844,21 @@ static int plan_enumerate(size_t n, size_t nt, const int *cands, int ncands, int
         if (force_nsplit > 0)
             s_lo = s_hi = (int)std::min<long long>(force_nsplit, ntl);
         for (int s = s_lo; s <= s_hi; s++) {
-            const double t1 = unit_time(cf, occ, ntl, 1, g_speed[c]);
-            const double ts = unit_time(cf, occ, ntl, s, g_speed[c]);
             // candidates (whole i-blocks, cost); s == 1: every block whole
             long long opt_full[2];
             double opt_t[2];
             int nopt = 0;
             if (s == 1) {
                 opt_full[nopt] = nb;
-                opt_t[nopt++] = std::ceil((double)nb / slots) * t1;
+                opt_t[nopt++] = plan_cost(cf, occ, d->sms, nb, ntl, 1, nb, g_speed[c]);
             } else {
                 const long long whole = force_nsplit > 0 ? 0 : (nb / slots) * slots;
                 if (whole > 0 && whole < nb) {  // tail-only split first: wins ties
                     opt_full[nopt] = whole;
-                    opt_t[nopt++] = (double)(whole / slots) * t1 +
-                                    std::ceil((double)(nb - whole) * s / slots) * ts;
+                    opt_t[nopt++] = plan_cost(cf, occ, d->sms, nb, ntl, s, whole, g_speed[c]);
                 }
                 opt_full[nopt] = 0;
-                opt_t[nopt++] = std::ceil((double)nb * s / slots) * ts;
+                opt_t[nopt++] = plan_cost(cf, occ, d->sms, nb, ntl, s, 0, g_speed[c]);
             }
             for (int k = 0; k < nopt; k++) {
                 const long long units = opt_full[k] + (nb - opt_full[k]) * s;
