@@ -251,3 +251,36 @@ def test_fused_epilogue_step_is_force_then_integrate(cuda, n, integrator):
     run(3)
     run(8)
     s.close()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 33, 257])
+def test_tiny_systems_one_launch_steps(cuda, n):
+    """Sizes far below one i-block or one j-tile (N = 1 has only its zero
+    self term): ten one-launch reference steps, each equal to the oracle's
+    CPU_AOS forces (within the force gate) and, on the GPU's own forces, the
+    oracle's integrator bit for bit; graph and direct steps agree."""
+    pm0, vm0 = nb.ic_reference(n, 3)
+    out = []
+    for graph in (True, False):
+        s = nb.System(n, nb.INTEGRATOR_REFERENCE, 0.01, 0.016, 0.95)
+        s.use_graph(graph)
+        s.set_state(pm0, vm0)
+        if graph:
+            s.step(8)  # one graph, then per-step checks below
+        for _ in range(2):
+            p_before, v_before = s.get_state()
+            s.step(1)
+            f = s.get_force()
+            ref = O.ieee().forces_aos(p_before, 0.01)
+            if n == 1:
+                assert np.all(f[:, :3] == 0)
+            else:
+                assert O.per_body_rel_error(f, ref)[0] <= TOL_FORCE
+            O.ieee().integrate(p_before, v_before, f, 0.016, 0.95)
+            p_after, v_after = s.get_state()
+            assert np.array_equal(p_after, p_before) and np.array_equal(v_after, v_before)
+        if not graph:
+            s.step(8)  # the same ten steps in another order of launches
+        out.append(s.get_state())
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
