@@ -90,8 +90,12 @@ NBGB_API size_t nbgb_force_workspace_bytes(size_t N);
 NBGB_API int nbgb_force(float *force, const float *posMass, float softeningSquared, size_t N,
                         void *workspace, size_t workspace_bytes, void *stream);
 
-/* As nbgb_force with the kernel configuration and j-split forced (-1 = the
-   planner's choice).  For tests and tuning. */
+/* As nbgb_force with the kernel configuration and j-split forced.  config:
+   -1 the planner's choice.  nsplit: -1 the planner's choice; > 0 every
+   i-block's j-range split nsplit ways; <= -2 whole i-blocks for the whole
+   rounds of CTA slots they fill and only the leftover i-blocks split
+   -nsplit ways (every i-block, when they fill no whole round).  For tests
+   and tuning. */
 NBGB_API int nbgb_force_ex(float *force, const float *posMass, float softeningSquared, size_t N,
                            void *workspace, size_t workspace_bytes, int config, int nsplit,
                            void *stream);
@@ -123,7 +127,8 @@ NBGB_API size_t nbgb_force_newton3_workspace_bytes(size_t N);
 NBGB_API int nbgb_force_newton3(float *force, const float *posMass, float softeningSquared,
                                 size_t N, void *workspace, size_t workspace_bytes, void *stream);
 
-/* The planner's decision for N (config / nsplit forced when >= 0). */
+/* The planner's decision for N (config forced when >= 0, nsplit as for
+   nbgb_force_ex). */
 NBGB_API int nbgb_force_plan(size_t N, int config, int nsplit, int *out_config, int *out_nsplit,
                              size_t *out_workspace_bytes);
 NBGB_API int nbgb_force_num_configs(void);

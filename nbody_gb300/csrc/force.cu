@@ -751,10 +751,10 @@ static void fill_layout(ForcePlan &pl, size_t n, size_t nt = 0) {
 }
 
 // Cost model, fitted to graph-timed sweeps of the log-domain configurations
-// x slice counts at N = 2,048-262,144 on GB300 (it picks a plan within 3.5 %
-// of the fastest measured one at every size; the earlier wave-count model
-// was up to 42 % off below N = 131,072).  Time is counted in interactions one
-// SM evaluates at full occupancy, scaled by the configuration's measured
+// x slice counts at N = 1,000-2^20 on GB300 (its plan is within 4 % of the
+// fastest measured one at every size; the earlier wave-count model was up to
+// 48 % off below N = 131,072).  Time is counted in interactions one SM
+// evaluates at full occupancy, scaled by the configuration's measured
 // relative speed.  Units are dealt to the SMs in rounds of `occ` co-resident
 // CTAs and a round lasts as long as its busiest SM: a full round runs occ
 // units at the SM's full throughput, a last partial round k units at the
@@ -763,15 +763,19 @@ static void fill_layout(ForcePlan &pl, size_t n, size_t nt = 0) {
 // nearly saturate the pipes, four do not).  Every round also pays a fixed
 // latency (the first j-tile's copy, the epilogue), every unit a small
 // overhead, and a split i-block's combining unit reads one partial per
-// slice.  For each configuration and slice count s > 1 two decompositions
-// are costed: every i-block split s ways, and only the i-blocks left over
-// after whole rounds of whole i-blocks split (nfull = whole rounds x slots).
-// Of the plans within 0.2 % of the cheapest, the one with the smallest
-// workspace wins (fewest partial sums, which then stay in L2).
+// slice.  SMs do not run at exactly the same speed, and the launch ends with
+// the slowest: a tenth of one final-round unit's time is added, so the last
+// units are kept short (at N = 2^20, the 224 leftover i-blocks split 19 ways
+// rather than 4: 0.6 % faster).  For each configuration and slice count
+// s > 1 two decompositions are costed: every i-block split s ways, and only
+// the i-blocks left over after whole rounds of whole i-blocks split
+// (nfull = whole rounds x slots).  Of the plans within 0.2 % of the
+// cheapest, the one with the smallest workspace wins.
 constexpr double kUnitOverhead = 9.0;      // sources per unit and target
 constexpr double kCombinePerSlice = 37.0;  // sources per slice and target, combining unit
 constexpr double kRoundLatency = 29800.0;  // about 1.5 us of one SM's interactions
 constexpr double kWarpTau = 1.8;
+constexpr double kLastUnitShare = 0.1;     // of one final-round unit's time
 
 static double sm_share(int k, int warps, int occ) {
     return (1.0 - std::exp(-(double)k * warps / kWarpTau)) /
@@ -779,14 +783,16 @@ static double sm_share(int k, int warps, int occ) {
 }
 
 // `units` equal units of `sources` sources x bi targets; *k_last: resident
-// units per SM in the last round.
+// units per SM in the last round; *unit_time: one unit's time in a full
+// round.
 static double rounds_time(long long units, double sources, double bi, int sms, int occ,
-                          int warps, double speed, int *k_last) {
+                          int warps, double speed, int *k_last, double *unit_time) {
     const long long slots = (long long)sms * occ;
     const double w = bi * (sources + kUnitOverhead) / speed;
     const long long full = units / slots, r = units % slots;
     double t = (double)full * (occ * w + kRoundLatency);
     *k_last = occ;
+    *unit_time = occ * w;
     if (r) {
         const int k = (int)((r + sms - 1) / sms);
         t += k * w / sm_share(k, warps, occ) + kRoundLatency;
@@ -799,21 +805,22 @@ static double rounds_time(long long units, double sources, double bi, int sms, i
 static double plan_cost(const ForceConfig &cf, int occ, int sms, long long nb, long long ntl,
                         int s, long long nfull, double speed) {
     const double bi = (double)cf.warps * 32 * cf.k;
-    double t = 0.0;
+    double t = 0.0, last_unit = 0.0;
     int k_last = occ;
     if (nfull > 0)
-        t += rounds_time(nfull, (double)ntl * cf.jt, bi, sms, occ, cf.warps, speed, &k_last);
+        t += rounds_time(nfull, (double)ntl * cf.jt, bi, sms, occ, cf.warps, speed, &k_last,
+                         &last_unit);
     if (nb > nfull) {
         if (s == 1) {
             t += rounds_time(nb - nfull, (double)ntl * cf.jt, bi, sms, occ, cf.warps, speed,
-                             &k_last);
+                             &k_last, &last_unit);
         } else {
             t += rounds_time((nb - nfull) * s, std::ceil((double)ntl / s) * cf.jt, bi, sms, occ,
-                             cf.warps, speed, &k_last);
+                             cf.warps, speed, &k_last, &last_unit);
             t += s * kCombinePerSlice * bi / (speed * sm_share(k_last, cf.warps, occ));
         }
     }
-    return t;
+    return t + kLastUnitShare * last_unit;
 }
 
 // Enumerates the candidate decompositions of n sources / nt targets over
@@ -840,9 +847,15 @@ static int plan_enumerate(size_t n, size_t nt, const int *cands, int ncands, int
         const long long bi = (long long)cf.warps * 32 * cf.k;
         const long long nb = ((long long)(nt ? nt : n) + bi - 1) / bi;
         const long long ntl = ((long long)n + cf.jt - 1) / cf.jt;
+        // force_nsplit > 0: every i-block split that many ways; <= -2: whole
+        // i-blocks for the whole rounds they fill, the rest split -force_nsplit
+        // ways (every i-block split when they fill no whole round)
+        const bool tail_only = force_nsplit <= -2;
         int s_lo = 1, s_hi = (int)std::min<long long>(ntl, 256);
-        if (force_nsplit > 0)
-            s_lo = s_hi = (int)std::min<long long>(force_nsplit, ntl);
+        if (force_nsplit > 0 || tail_only)
+            s_lo = s_hi = (int)std::min<long long>(tail_only ? -(long long)force_nsplit
+                                                             : (long long)force_nsplit,
+                                                   ntl);
         for (int s = s_lo; s <= s_hi; s++) {
             // candidates (whole i-blocks, cost); s == 1: every block whole
             long long opt_full[2];
@@ -853,12 +866,15 @@ static int plan_enumerate(size_t n, size_t nt, const int *cands, int ncands, int
                 opt_t[nopt++] = plan_cost(cf, occ, d->sms, nb, ntl, 1, nb, g_speed[c]);
             } else {
                 const long long whole = force_nsplit > 0 ? 0 : (nb / slots) * slots;
-                if (whole > 0 && whole < nb) {  // tail-only split first: wins ties
+                const bool has_tail = whole > 0 && whole < nb;
+                if (has_tail) {  // tail-only split first: wins ties
                     opt_full[nopt] = whole;
                     opt_t[nopt++] = plan_cost(cf, occ, d->sms, nb, ntl, s, whole, g_speed[c]);
                 }
-                opt_full[nopt] = 0;
-                opt_t[nopt++] = plan_cost(cf, occ, d->sms, nb, ntl, s, 0, g_speed[c]);
+                if (!(tail_only && has_tail)) {
+                    opt_full[nopt] = 0;
+                    opt_t[nopt++] = plan_cost(cf, occ, d->sms, nb, ntl, s, 0, g_speed[c]);
+                }
             }
             for (int k = 0; k < nopt; k++) {
                 const long long units = opt_full[k] + (nb - opt_full[k]) * s;

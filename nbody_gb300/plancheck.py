@@ -3,12 +3,14 @@
     python -m nbody_gb300.plancheck [--sizes 1000,4096,...] [--calls 5]
 
 For each N (a seeded Plummer sphere) it times the planner's own plan for
-nbgb_force and a grid of forced plans (configuration x slice count, every
-i-block split), each as a CUDA graph of `calls` back-to-back calls (the pack
-and force kernels, no host work in the timed region), and prints one JSON
-line per N: the planner's plan and time, the fastest three grid plans and the
-planner's time over the fastest.  Plans change speed only; results differ at
-most by rounding.
+nbgb_force and a grid of forced plans (configuration x slice count: every
+i-block split s ways, and from N = 131,072 also whole i-blocks for the whole
+rounds of CTA slots plus the leftover i-blocks split s ways, nsplit = -s),
+each as a CUDA graph of `calls` back-to-back calls (the pack and force
+kernels, no host work in the timed region), and prints one JSON line per N:
+the planner's plan and time, the fastest three grid plans and the planner's
+time over the fastest.  Plans change speed only; results differ at most by
+rounding.
 """
 from __future__ import annotations
 
@@ -22,6 +24,7 @@ DEFAULT_SIZES = (1000, 2048, 3000, 4096, 6000, 8192, 10007, 12000, 16384, 20000,
 GRID_CONFIGS = ("w8_k2_jt1024_s3_log4", "w4_k2_jt256_s4_log4", "w8_k2_jt256_s4_log4",
                 "w8_k2_jt2048_s2_log4", "w6_k3_jt1024_s2_log4")
 GRID_SPLITS = (1, 4, 8, 16, 32)
+TAIL_SPLITS = (-8, -16, -32)  # leftover i-blocks only, from N = 131,072
 
 
 def graph_time_us(pm, out, config: int, nsplit: int, calls: int, reps: int = 3) -> float:
@@ -63,12 +66,13 @@ def check(n: int, calls: int = 5) -> dict:
     cfg, nsplit, wsb = force_plan(n)
     t_plan = graph_time_us(pm, out, -1, -1, calls)
     large = n > 262144  # few grid points: these sizes take 0.1-0.4 s a call
+    tails = TAIL_SPLITS if n >= 131072 else ()
     grid = []
-    for name in (GRID_CONFIGS[:1] if large else GRID_CONFIGS):
+    for ci, name in enumerate(GRID_CONFIGS[:1] if large else GRID_CONFIGS):
         c = names.index(name)
-        for s in ((8, 16) if large else GRID_SPLITS):
+        for s in ((8, 16) if large else GRID_SPLITS) + (tails if ci == 0 else ()):
             _, s_eff, _ = force_plan(n, c, s)
-            if s_eff != s:
+            if s_eff != abs(s):
                 continue  # fewer j-tiles than slices
             grid.append((graph_time_us(pm, out, c, s, 2 if large else calls), name, s))
     grid.sort()
