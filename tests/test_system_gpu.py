@@ -284,3 +284,25 @@ def test_tiny_systems_one_launch_steps(cuda, n):
         out.append(s.get_state())
         s.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_fused_epilogue_step_at_the_headline_size(cuda):
+    """N = 2^20 (the plan takes whole i-blocks for the first rounds and splits
+    the leftover i-blocks into many slices): two one-launch reference steps,
+    each equal to the standalone force kernel on that step's positions and
+    the reference integrator (contracted drift), bit for bit."""
+    import torch
+    n = 1 << 20
+    _, _, pm0, vm0 = nb.ic_plummer(n, 2)  # velInvMass.w = 1/m
+    s = nb.System(n, nb.INTEGRATOR_REFERENCE_FUSED, 1e-4, 0.005, 1.0)
+    assert s.plan() == nb.force_plan(n)[:2]
+    s.set_state(pm0, vm0)
+    p, v = pm0.copy(), vm0.copy()
+    for _ in range(2):
+        f = nb.force(torch.from_numpy(p).cuda(), 1e-4).cpu().numpy()
+        O.ieee().integrate_contracted(p, v, f, 0.005, 1.0)
+        s.step(1)
+        ps, vs = s.get_state()
+        assert np.array_equal(ps, p) and np.array_equal(vs, v)
+        assert np.array_equal(s.get_force()[:, :3], f[:, :3])
+    s.close()
