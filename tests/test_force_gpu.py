@@ -197,6 +197,24 @@ def test_tail_split_plans(cuda, n):
     assert np.array_equal(_gpu_force(pm, 1e-4), out)  # deterministic
 
 
+def test_forced_tail_only_splits(cuda):
+    """nsplit <= -2 forces whole i-blocks for the whole rounds of CTA slots
+    and only the leftover i-blocks split -nsplit ways: a different workspace
+    from splitting every i-block, results equal to the unsplit plan to
+    rounding, deterministic."""
+    n = 311300
+    _, _, pm, _ = nb.ic_plummer(n, 5)
+    cfg = nb.force_config_names().index("w8_k2_jt1024_s3_log4")
+    _, s_tail, ws_tail = nb.force_plan(n, cfg, -16)
+    _, s_all, ws_all = nb.force_plan(n, cfg, 16)
+    assert s_tail == s_all == 16 and ws_tail < ws_all
+    whole = _gpu_force(pm, 1e-4, config=cfg, nsplit=1)
+    for ns in (-2, -16, -64):
+        out = _gpu_force(pm, 1e-4, config=cfg, nsplit=ns)
+        assert O.per_body_rel_error(out, whole)[0] <= 1e-6, ns
+        assert np.array_equal(_gpu_force(pm, 1e-4, config=cfg, nsplit=ns), out)
+
+
 def test_split_choice_changes_only_rounding(cuda):
     g = golden("ball2048")
     a = _gpu_force(g["posMass"], 1e-4, 0, 1)
