@@ -124,24 +124,36 @@ int ensure_jstream(nbgb_system *s) {
     return rc;
 }
 
-// Reference integrators: the second j-stream buffer, sized for the plan and
-// packed once so its zero-mass padding is in place (the fused integrate
-// writes the real bodies' entries every step).
-int ensure_js2(nbgb_system *s) {
-    const size_t bytes =
-        (size_t)s->plan.ntiles * s->plan.tile_bodies * 16 * (size_t)s->plan.js_vpb;
-    if (s->js2_ready && s->js2_bytes == bytes)
+size_t js_bytes(const nbgb::ForcePlan &pl) {
+    return (size_t)pl.ntiles * pl.tile_bodies * 16 * (size_t)pl.js_vpb;
+}
+
+// Reference integrators: the second j-stream buffer, allocated with the
+// system and whenever the plan changes (never inside a step, so steps can be
+// captured by the caller), large enough for the plan.
+int alloc_js2(nbgb_system *s) {
+    const size_t bytes = js_bytes(s->plan);
+    s->js2_ready = false;
+    if (s->js2 && s->js2_bytes >= bytes)
         return NBGB_OK;
-    if (s->js2_bytes != bytes) {
-        cudaFree(s->js2);
+    cudaFree(s->js2);
+    s->js2 = nullptr;
+    s->js2_bytes = 0;
+    if (cudaMalloc(&s->js2, bytes) != cudaSuccess) {
         s->js2 = nullptr;
-        s->js2_bytes = 0;
-        if (cudaMalloc(&s->js2, bytes) != cudaSuccess) {
-            s->js2 = nullptr;
-            return NBGB_ERR_NO_MEMORY;
-        }
-        s->js2_bytes = bytes;
+        return NBGB_ERR_NO_MEMORY;
     }
+    s->js2_bytes = bytes;
+    return NBGB_OK;
+}
+
+// Packed once per plan so its zero-mass padding is in place (the fused
+// integrate writes the real bodies' entries every step).
+int ensure_js2(nbgb_system *s) {
+    if (s->js2_ready)
+        return NBGB_OK;
+    if (!s->js2 || s->js2_bytes < js_bytes(s->plan))
+        return NBGB_ERR_INVALID_ARGUMENT;
     int rc = nbgb::launch_pack(s->plan, s->pm, s->ws, s->stream, s->js2);
     if (rc == NBGB_OK)
         s->js2_ready = true;
@@ -276,8 +288,9 @@ int fit_plan_to_masses(nbgb_system *s, const float *m, size_t stride) {
         return NBGB_ERR_CUDA;
     drop_graphs(s);
     s->plan = pl;
-    s->js2_ready = false;  // repacked (and resized) for the new plan
     s->js_cur = 0;
+    if (reference_integrator(s->integrator) && (rc = alloc_js2(s)) != NBGB_OK)
+        return rc;  // repacked for the new plan at the next step
     return NBGB_OK;
 }
 
@@ -396,6 +409,7 @@ NBGB_API nbgb_system *nbgb_system_create(size_t N, int integrator, float softeni
     s->ws_bytes = s->plan.workspace_bytes;
     if (reference_integrator(integrator)) {
         ok = ok && cudaMalloc(&s->vel, N * 16) == cudaSuccess;
+        ok = ok && alloc_js2(s) == NBGB_OK;
     } else {
         s->ld = (N + 63) / 64 * 64;
         ok = ok && cudaMalloc(&s->x64, s->ld * 6 * sizeof(double)) == cudaSuccess;
