@@ -1,7 +1,6 @@
 """Failure handling without a GPU fault: a bounded wait runs out on purpose
 (an mbarrier nothing completes, 20 ms limit), the kernel reports it in the
 device status word and returns, and the context stays usable."""
-import numpy as np
 import pytest
 
 import nbody_gb300 as nb

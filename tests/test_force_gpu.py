@@ -1,7 +1,5 @@
 """Parity of the GB300 force kernel against the reference's CPU_AOS outputs
 (golden fixtures), the CPU oracle and an FP64 all-pairs sum."""
-import ctypes
-
 import numpy as np
 import pytest
 
