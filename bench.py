@@ -30,6 +30,10 @@ interaction (src/nbody.cu:1027).
             sample, per body against the FP64 all-pairs sum and against the
             oracle's CPU_AOS restatements (IEEE and the reference's flags),
             computed outside every timed region
+  reference_mode  milliseconds per resident reference-mode step on small
+            plain systems (N = 1,024, 4,096, 16,384): one launch per step
+            (the integrate in the force kernel's epilogue) against force
+            then integrate, both replaying CUDA graphs of 8 steps
 
 --impl reference times the reference's CPU implementation of the path (the
 reference's own compiled CPU_SOA when oracle/_ref was built on this machine,
