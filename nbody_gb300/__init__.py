@@ -97,6 +97,8 @@ def release_workspace() -> None:
 # Stream-ordered force
 # ---------------------------------------------------------------------------
 def force_plan(N: int, config: int = -1, nsplit: int = -1):
+    """(configuration, slice count, workspace bytes) of the plan nbgb_force
+    runs for N (config / nsplit as for force())."""
     c, s, w = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
     check(load().nbgb_force_plan(N, config, nsplit, ctypes.byref(c), ctypes.byref(s),
                                  ctypes.byref(w)), "nbgb_force_plan")
@@ -127,7 +129,10 @@ _default_ws = Workspace()
 def force(posMass, softeningSquared: float, out=None, stream=None, workspace: Workspace = None,
           config: int = -1, nsplit: int = -1):
     """F_i = sum_j m_j d_ij / (|d_ij|^2 + eps2)^1.5 for a (N,4) float32 CUDA
-    tensor {x,y,z,m}; returns (N,4) {fx,fy,fz,0}."""
+    tensor {x,y,z,m}; returns (N,4) {fx,fy,fz,0}.  config / nsplit force a
+    plan (-1: the planner's choice; nsplit > 0 splits every i-block's
+    sources nsplit ways, nsplit <= -2 only the i-blocks left over after
+    whole rounds of CTA slots, -nsplit ways)."""
     torch = _torch()
     n = posMass.shape[0]
     if out is None:
