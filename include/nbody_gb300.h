@@ -131,6 +131,15 @@ NBGB_API int nbgb_force_newton3(float *force, const float *posMass, float soften
    nbgb_force_ex). */
 NBGB_API int nbgb_force_plan(size_t N, int config, int nsplit, int *out_config, int *out_nsplit,
                              size_t *out_workspace_bytes);
+/* The same decision without a GPU, for a device with `sms` SMs and
+   occupancy[c] resident CTAs per SM of configuration c (nconfigs must equal
+   nbgb_force_num_configs()); out_nfull: i-blocks kept whole. */
+NBGB_API int nbgb_force_plan_on(size_t N, int sms, const int *occupancy, int nconfigs, int config,
+                                int nsplit, int *out_config, int *out_nsplit, int *out_nfull,
+                                size_t *out_workspace_bytes);
+/* The current device's SM count and resident CTAs per SM of every
+   configuration, as the planner uses them (nconfigs >= the number). */
+NBGB_API int nbgb_force_device_info(int *sms, int *occupancy, int nconfigs);
 NBGB_API int nbgb_force_num_configs(void);
 NBGB_API const char *nbgb_force_config_name(int config);
 /* Relative throughput the planner assumes for a configuration (measured

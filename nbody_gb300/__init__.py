@@ -105,6 +105,30 @@ def force_plan(N: int, config: int = -1, nsplit: int = -1):
     return c.value, s.value, w.value
 
 
+def force_plan_on(N: int, sms: int, occupancy, config: int = -1, nsplit: int = -1):
+    """The planner's decision for N on a device with `sms` SMs and
+    occupancy[c] resident CTAs per SM of configuration c, without a GPU:
+    (configuration, slice count, whole i-blocks, workspace bytes)."""
+    lib = load()
+    occ = (ctypes.c_int * len(occupancy))(*[int(x) for x in occupancy])
+    c, s, f, w = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+    check(lib.nbgb_force_plan_on(N, sms, occ, len(occupancy), config, nsplit, ctypes.byref(c),
+                                 ctypes.byref(s), ctypes.byref(f), ctypes.byref(w)),
+          "nbgb_force_plan_on")
+    return c.value, s.value, f.value, w.value
+
+
+def force_device_info():
+    """(SM count, resident CTAs per SM of every configuration) of the current
+    device, as the planner sees them."""
+    lib = load()
+    n = lib.nbgb_force_num_configs()
+    occ = (ctypes.c_int * n)()
+    sms = ctypes.c_int()
+    check(lib.nbgb_force_device_info(ctypes.byref(sms), occ, n), "nbgb_force_device_info")
+    return sms.value, list(occ)
+
+
 def force_config_names():
     lib = load()
     return [lib.nbgb_force_config_name(i).decode() for i in range(lib.nbgb_force_num_configs())]

@@ -34,6 +34,10 @@ SIGNATURES = {
                                           c_vp]),
     "nbgb_force_plan": (ctypes.c_int, [c_size, ctypes.c_int, ctypes.c_int, c_intp, c_intp,
                                        c_sizep]),
+    "nbgb_force_plan_on": (ctypes.c_int, [c_size, ctypes.c_int, c_intp, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, c_intp, c_intp, c_intp,
+                                          c_sizep]),
+    "nbgb_force_device_info": (ctypes.c_int, [c_intp, c_intp, ctypes.c_int]),
     "nbgb_force_num_configs": (ctypes.c_int, []),
     "nbgb_force_config_name": (ctypes.c_char_p, [ctypes.c_int]),
     "nbgb_force_set_speed": (ctypes.c_int, [ctypes.c_int, ctypes.c_double]),

@@ -829,10 +829,13 @@ static double plan_cost(const ForceConfig &cf, int occ, int sms, long long nb, l
 // workspace (fewest partial sums) is written to pl.
 constexpr double kPlanTie = 2e-3;
 
+// d: the device's SM count and resident CTAs per configuration (the current
+// device's when null).
 template <typename Keep>
 static int plan_enumerate(size_t n, size_t nt, const int *cands, int ncands, int force_nsplit,
-                          ForcePlan &pl, Keep keep) {
-    const DeviceInfo *d = device_info();
+                          ForcePlan &pl, Keep keep, const DeviceInfo *d = nullptr) {
+    if (!d)
+        d = device_info();
     if (!d)
         return NBGB_ERR_CUDA;
     std::vector<std::pair<double, ForcePlan>> kept;
@@ -904,12 +907,14 @@ static int plan_enumerate(size_t n, size_t nt, const int *cands, int ncands, int
 }
 
 static int plan_force_among(size_t n, const std::vector<int> &cands, int force_nsplit,
-                            ForcePlan &pl, size_t nt = 0) {
-    return plan_enumerate(n, nt, cands.data(), (int)cands.size(), force_nsplit, pl,
-                          [](const ForcePlan &) { return true; });
+                            ForcePlan &pl, size_t nt = 0, const DeviceInfo *d = nullptr) {
+    return plan_enumerate(
+        n, nt, cands.data(), (int)cands.size(), force_nsplit, pl,
+        [](const ForcePlan &) { return true; }, d);
 }
 
-int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
+static int plan_force_on(size_t n, int force_config, int force_nsplit, ForcePlan &pl,
+                         const DeviceInfo *d) {
     if (n == 0 || n > kMaxBodies)
         return NBGB_ERR_INVALID_ARGUMENT;
     std::vector<int> cands;
@@ -920,7 +925,11 @@ int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
     } else {
         cands.assign(std::begin(kDefaultCandidates), std::end(kDefaultCandidates));
     }
-    return plan_force_among(n, cands, force_nsplit, pl);
+    return plan_force_among(n, cands, force_nsplit, pl, 0, d);
+}
+
+int plan_force(size_t n, int force_config, int force_nsplit, ForcePlan &pl) {
+    return plan_force_on(n, force_config, force_nsplit, pl, nullptr);
 }
 
 int plan_force_rows(size_t n, size_t rows, ForcePlan &pl) {
@@ -1106,6 +1115,51 @@ NBGB_API size_t nbgb_force_workspace_bytes(size_t N) {
     if (plan_force(N, -1, -1, pl) != NBGB_OK)
         return 0;
     return pl.workspace_bytes;
+}
+
+// The planner without a GPU: the same decision for a device with `sms` SMs
+// and occupancy[c] resident CTAs per SM of configuration c (all
+// configurations; nbgb_force_device_info reports a real device's).
+NBGB_API int nbgb_force_plan_on(size_t N, int sms, const int *occupancy, int nconfigs, int config,
+                                int nsplit, int *out_config, int *out_nsplit, int *out_nfull,
+                                size_t *out_workspace_bytes) {
+    if (sms <= 0 || !occupancy || nconfigs != kNumConfigs)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    DeviceInfo d;
+    d.sms = sms;
+    for (int c = 0; c < kNumConfigs; c++) {
+        if (occupancy[c] < 0)
+            return NBGB_ERR_INVALID_ARGUMENT;
+        d.occ[c] = occupancy[c];
+    }
+    d.ok = true;
+    ForcePlan pl;
+    int rc = plan_force_on(N, config, nsplit, pl, &d);
+    if (rc != NBGB_OK)
+        return rc;
+    if (out_config)
+        *out_config = pl.config;
+    if (out_nsplit)
+        *out_nsplit = pl.nsplit;
+    if (out_nfull)
+        *out_nfull = pl.nfull;
+    if (out_workspace_bytes)
+        *out_workspace_bytes = pl.workspace_bytes;
+    return NBGB_OK;
+}
+
+// The current device's SM count and resident CTAs per SM of every
+// configuration (as the planner sees them).
+NBGB_API int nbgb_force_device_info(int *sms, int *occupancy, int nconfigs) {
+    if (!sms || !occupancy || nconfigs < kNumConfigs)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    const DeviceInfo *d = device_info();
+    if (!d)
+        return NBGB_ERR_CUDA;
+    *sms = d->sms;
+    for (int c = 0; c < kNumConfigs; c++)
+        occupancy[c] = d->occ[c];
+    return NBGB_OK;
 }
 
 NBGB_API int nbgb_force_plan(size_t N, int config, int nsplit, int *out_config, int *out_nsplit,
