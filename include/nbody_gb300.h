@@ -261,6 +261,11 @@ NBGB_API void *nbgb_system_device_posmass(nbgb_system *sys);
 NBGB_API void *nbgb_system_device_force(nbgb_system *sys);
 NBGB_API void *nbgb_system_stream(nbgb_system *sys);
 NBGB_API int nbgb_system_plan(nbgb_system *sys, int *config, int *nsplit);
+/* Force the one-sided kernel's plan (config / nsplit as for nbgb_force_ex;
+   -1, -1 restores the planner's choice).  For tuning and tests; the
+   potential configuration is refused, log-domain configurations need
+   masses >= 0.  Synchronises the system's stream. */
+NBGB_API int nbgb_system_set_plan(nbgb_system *sys, int config, int nsplit);
 
 /* ======================================================================== */
 /* Ensembles of independent systems (batched and served)                     */

@@ -353,6 +353,11 @@ class System:
         return {"kinetic": out[0], "potential": out[1], "energy": out[0] + out[1],
                 "momentum": out[2:5].copy(), "angular_momentum": out[5:8].copy()}
 
+    def set_plan(self, config: int = -1, nsplit: int = -1):
+        """Force the one-sided kernel's plan (as for force(); -1, -1: the
+        planner's choice)."""
+        check(self.lib.nbgb_system_set_plan(self.h, config, nsplit), "set_plan")
+
     def plan(self):
         c, s = ctypes.c_int(), ctypes.c_int()
         check(self.lib.nbgb_system_plan(self.h, ctypes.byref(c), ctypes.byref(s)), "plan")

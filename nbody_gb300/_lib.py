@@ -72,6 +72,7 @@ SIGNATURES = {
     "nbgb_system_device_force": (c_vp, [c_vp]),
     "nbgb_system_stream": (c_vp, [c_vp]),
     "nbgb_system_plan": (ctypes.c_int, [c_vp, c_intp, c_intp]),
+    "nbgb_system_set_plan": (ctypes.c_int, [c_vp, ctypes.c_int, ctypes.c_int]),
     "nbgb_ensemble_create": (c_vp, [c_size, ctypes.c_int, ctypes.c_float]),
     "nbgb_ensemble_destroy": (None, [c_vp]),
     "nbgb_ensemble_device_bytes": (c_size, [c_vp]),

@@ -773,6 +773,43 @@ NBGB_API int nbgb_system_diagnostics(nbgb_system *s, double *out) {
 NBGB_API void *nbgb_system_device_posmass(nbgb_system *s) { return s ? s->pm : nullptr; }
 NBGB_API void *nbgb_system_device_force(nbgb_system *s) { return s ? s->force : nullptr; }
 NBGB_API void *nbgb_system_stream(nbgb_system *s) { return s ? s->stream : nullptr; }
+// Force plan of the one-sided kernel: config / nsplit as for nbgb_force_ex
+// (-1, -1: the planner's choice again).  For tuning and tests.  The
+// potential configuration is refused; log-domain configurations need masses
+// >= 0.  KDK: a pending closing half kick is applied first and the next step
+// starts with a force pass under the new plan.
+NBGB_API int nbgb_system_set_plan(nbgb_system *s, int config, int nsplit) {
+    if (!s || config == nbgb::kPotentialConfig)
+        return NBGB_ERR_INVALID_ARGUMENT;
+    nbgb::ForcePlan pl;
+    int rc = nbgb::plan_force(s->n, config, nsplit, pl);
+    if (rc != NBGB_OK)
+        return rc;
+    if ((rc = sync_velocities(s)) != NBGB_OK)
+        return rc;
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    if (pl.workspace_bytes > s->ws_bytes) {
+        void *ws = nullptr;
+        if (cudaMalloc(&ws, pl.workspace_bytes) != cudaSuccess)
+            return NBGB_ERR_NO_MEMORY;
+        cudaFree(s->ws);
+        s->ws = ws;
+        s->ws_bytes = pl.workspace_bytes;
+    }
+    // split counters start at zero
+    if (cudaMemsetAsync(s->ws, 0, s->ws_bytes, s->stream) != cudaSuccess)
+        return NBGB_ERR_CUDA;
+    drop_graphs(s);
+    s->plan = pl;
+    s->js_cur = 0;
+    s->js_valid = false;  // repacked in the new layout at the next step
+    s->accel_valid = false;
+    if (reference_integrator(s->integrator) && (rc = alloc_js2(s)) != NBGB_OK)
+        return rc;
+    return NBGB_OK;
+}
+
 NBGB_API int nbgb_system_plan(nbgb_system *s, int *config, int *nsplit) {
     if (!s)
         return NBGB_ERR_INVALID_ARGUMENT;

@@ -306,3 +306,47 @@ def test_fused_epilogue_step_at_the_headline_size(cuda):
         assert np.array_equal(ps, p) and np.array_equal(vs, v)
         assert np.array_equal(s.get_force()[:, :3], f[:, :3])
     s.close()
+
+
+@pytest.mark.parametrize("config_name", ["w8_k4_jt512_s3_f32", "w8_k2_jt256_s4_f32x2",
+                                         "w8_k2_jt256_s4_fma2", "w8_k4_jt256_s4_tpair",
+                                         "w8_k2_jt1024_s3_log4", "w8_k2_jt1024_s2_pf_log4"])
+@pytest.mark.parametrize("nsplit", [1, 3])
+def test_fused_epilogue_in_every_kernel_mode(cuda, config_name, nsplit):
+    """The integrate fused into the force epilogue under every kernel mode
+    (scalar, f32x2, all-FMA, target pairs with the duplicated source layout,
+    log-domain pairs, prefetching) and with and without a j-split, forced
+    with System.set_plan: each step equals the standalone kernel of the same
+    plan followed by the reference integrator, bit for bit."""
+    n = 5003
+    cfg = nb.force_config_names().index(config_name)
+    pm0, vm0 = nb.ic_reference(n, 21)
+    s = nb.System(n, nb.INTEGRATOR_REFERENCE, 0.01, 0.016, 0.95)
+    s.set_plan(cfg, nsplit)
+    assert s.plan() == nb.force_plan(n, cfg, nsplit)[:2]
+    s.set_state(pm0, vm0)
+    p, v = pm0.copy(), vm0.copy()
+
+    def forced(t):
+        return nb.force(t, 0.01, config=cfg, nsplit=nsplit)
+
+    for m in (1, 2, 8):  # direct steps from either buffer, then one graph
+        f = _host_steps(p, v, m, False, forced)
+        s.step(m)
+        ps, vs = s.get_state()
+        assert np.array_equal(ps, p) and np.array_equal(vs, v), (config_name, nsplit, m)
+        assert np.array_equal(s.get_force()[:, :3], f[:, :3])
+    s.set_plan()  # back to the planner's choice, mid-run
+    assert s.plan() == nb.force_plan(n)[:2]
+    f = _host_steps(p, v, 2, False, lambda t: nb.force(t, 0.01))
+    s.step(2)
+    ps, vs = s.get_state()
+    assert np.array_equal(ps, p) and np.array_equal(vs, v)
+    s.close()
+
+
+def test_set_plan_rejects_the_potential_configuration(cuda):
+    s = nb.System(1000, nb.INTEGRATOR_REFERENCE, 0.01, 0.016, 0.95)
+    with pytest.raises(nb.NbgbError):
+        s.set_plan(nb.force_config_names().index("w8_k2_jt256_s4_pot"), 1)
+    s.close()
