@@ -350,3 +350,25 @@ def test_set_plan_rejects_the_potential_configuration(cuda):
     with pytest.raises(nb.NbgbError):
         s.set_plan(nb.force_config_names().index("w8_k2_jt256_s4_pot"), 1)
     s.close()
+
+
+@pytest.mark.parametrize("config_name", ["w8_k4_jt256_s4_tpair", "w8_k2_jt256_s4_f32x2",
+                                         "w8_k2_jt1024_s3_log4"])
+def test_kdk64_under_forced_plans(cuda, config_name):
+    """FP64 KDK steps write the next j-stream in the plan's layout (paired or
+    duplicated sources, log-domain slots): under each forced plan the
+    trajectory follows the default plan's to force rounding."""
+    n = 3001
+    p0, v0, pm, _ = nb.ic_plummer(n, 9)
+    m = pm[:, 3].copy()
+    out = []
+    for cfg in (-1, nb.force_config_names().index(config_name)):
+        s = nb.System(n, nb.INTEGRATOR_KDK64, 1e-4, 0.002, 1.0)
+        s.set_plan(cfg, 2 if cfg >= 0 else -1)
+        s.set_state64(p0, v0, m)
+        s.step(10)
+        out.append(s.get_state64())
+        s.close()
+    dp = np.abs(out[0][0] - out[1][0]).max()
+    dv = np.abs(out[0][1] - out[1][1]).max() / np.abs(out[0][1]).max()
+    assert dp < 1e-9 and dv < 1e-6, (dp, dv)
