@@ -76,44 +76,18 @@ struct ForceParams {
 // ---------------------------------------------------------------------------
 // pack: AOS -> paired j-stream, zero-mass padding, counter reset.
 // ---------------------------------------------------------------------------
-// logm != 0 (mode 6 plans): pairs q with q % 4 == 0 carry log2 of their
-// masses (jstream_log_mass) instead of the masses.
+// One body per thread (coalesced loads; the pairs are assembled with a lane
+// swap, store_jstream_body), vpb 1 paired or 2 duplicated layout.  logm != 0
+// (log-domain plans): pairs q with q % 4 == 0 carry log2 of their masses
+// (jstream_log_mass) instead of the masses.
 __global__ void pack_jstream_kernel(const float4 *__restrict__ pm, float4 *__restrict__ js, int n,
                                     int npad, unsigned *__restrict__ counters, int ncounters,
-                                    int logm) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // pair index
-    if (q < ncounters)
-        counters[q] = 0u;
-    if (2 * q >= npad)
-        return;
-    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 b0 = (2 * q < n) ? pm[2 * q] : z;
-    float4 b1 = (2 * q + 1 < n) ? pm[2 * q + 1] : z;
-    if (logm && jstream_log_slot(q)) {
-        b0.w = jstream_log_mass(b0.w);
-        b1.w = jstream_log_mass(b1.w);
-    }
-    js[2 * q] = make_float4(b0.x, b1.x, b0.y, b1.y);
-    js[2 * q + 1] = make_float4(b0.z, b1.z, b0.w, b1.w);
-}
-
-// pack, duplicated layout: body j -> {xj,xj,yj,yj},{zj,zj,mj,mj} (32 B), for
-// kernels that pair two targets per f32x2 register instead of two sources.
-__global__ void pack_jstream_dup_kernel(const float4 *__restrict__ pm, float4 *__restrict__ js,
-                                        int n, int npad, unsigned *__restrict__ counters,
-                                        int ncounters) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // pair of bodies
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int j = 2 * q + h;
-        if (j >= npad)
-            break;
-        const float4 b = (j < n) ? pm[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        js[2 * j] = make_float4(b.x, b.x, b.y, b.y);
-        js[2 * j + 1] = make_float4(b.z, b.z, b.w, b.w);
-    }
-    if (q < ncounters)
-        counters[q] = 0u;
+                                    int vpb, int logm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // body
+    if (i < ncounters)
+        counters[i] = 0u;
+    const float4 b = (i < n) ? pm[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    store_jstream_body(js, vpb, logm, i, b, i < npad);
 }
 
 // The reference integrator (integrateOne, src/nbody.cu:158-182) applied to
@@ -1002,14 +976,10 @@ int launch_pack(const ForcePlan &pl, const float4 *posMass, void *workspace, cud
     unsigned *cnt = (!js_out && split_blocks(pl)) ? (unsigned *)(ws + pl.off_cnt) : nullptr;
     const int npad = pl.ntiles * pl.tile_bodies;
     const int ncnt = cnt ? split_blocks(pl) : 0;
-    const int work = std::max(npad / 2, ncnt);
+    const int work = std::max(npad, ncnt);
     const int tb = 256;
-    if (pl.js_vpb == 2)
-        pack_jstream_dup_kernel<<<(work + tb - 1) / tb, tb, 0, stream>>>(posMass, js, (int)pl.n,
-                                                                          npad, cnt, ncnt);
-    else
-        pack_jstream_kernel<<<(work + tb - 1) / tb, tb, 0, stream>>>(posMass, js, (int)pl.n, npad,
-                                                                      cnt, ncnt, pl.js_log);
+    pack_jstream_kernel<<<(work + tb - 1) / tb, tb, 0, stream>>>(posMass, js, (int)pl.n, npad, cnt,
+                                                                  ncnt, pl.js_vpb, pl.js_log);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 

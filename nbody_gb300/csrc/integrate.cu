@@ -26,9 +26,11 @@
 //               posMass 16, j-stream 16)
 //   half_kick   v += a * dt/2, closing a leapfrog step (64 B per body: read
 //               v 24, a 16; write v 24)
-// Each thread owns one body pair (2q, 2q+1): FP64 components move as one
-// 16-byte double2, FP32 masses as one float2, so every access is a 128-bit
-// (or 64-bit) coalesced vector access.  GB300's FP64 pipe is narrow (~1.7
+// Each thread owns one body, consecutive threads consecutive bodies, so every
+// access of a warp is one contiguous run (float4 AOS: 512 B; FP64 SoA: 256 B;
+// a thread owning a body pair instead made every float4 access a 32-byte
+// stride, 25 % slower on GB300); the j-stream's source pairs are assembled
+// with a lane swap.  GB300's FP64 pipe is narrow (~1.7
 // operations per SM per clock), so the kernels keep FP64 for the updates
 // themselves (6 DFMA per body in kick_drift, 3 in half_kick) and do the
 // FP32 <-> FP64 conversions on the integer pipe (widen_f32 / narrow_f64,
@@ -47,26 +49,6 @@ namespace nbgb {
 
 constexpr int kIntegrateThreads = 256;
 
-// j-stream store for bodies 2q, 2q+1 in either layout (vpb 1: source pairs,
-// vpb 2: each source duplicated); logm: log2 masses in the pairs that carry
-// them in log-domain plans.
-__device__ __forceinline__ void store_jstream(float4 *__restrict__ js, int vpb, int logm, int q,
-                                              float4 b0, float4 b1) {
-    if (logm && jstream_log_slot(q)) {
-        b0.w = jstream_log_mass(b0.w);
-        b1.w = jstream_log_mass(b1.w);
-    }
-    if (vpb == 2) {
-        js[4 * q] = make_float4(b0.x, b0.x, b0.y, b0.y);
-        js[4 * q + 1] = make_float4(b0.z, b0.z, b0.w, b0.w);
-        js[4 * q + 2] = make_float4(b1.x, b1.x, b1.y, b1.y);
-        js[4 * q + 3] = make_float4(b1.z, b1.z, b1.w, b1.w);
-    } else {
-        js[2 * q] = make_float4(b0.x, b1.x, b0.y, b1.y);
-        js[2 * q + 1] = make_float4(b0.z, b1.z, b0.w, b1.w);
-    }
-}
-
 template <bool FUSED_DRIFT>
 __device__ __forceinline__ float drift(float x, float v, float dt) {
     if constexpr (FUSED_DRIFT)
@@ -75,138 +57,92 @@ __device__ __forceinline__ float drift(float x, float v, float dt) {
         return __fadd_rn(x, __fmul_rn(v, dt));
 }
 
-// Thread q owns bodies 2q and 2q+1 (one j-stream pair).
+// One body per thread (i = global thread index; consecutive threads on
+// consecutive bodies, so every float4 access is coalesced); the j-stream
+// pairs are assembled with a lane swap (store_jstream_body).
 template <bool FUSED_DRIFT>
 __global__ void __launch_bounds__(kIntegrateThreads)
     integrate_reference_kernel(float4 *__restrict__ pm, float4 *__restrict__ vel,
                                const float4 *__restrict__ force, float dt, float damping, int n,
                                float4 *__restrict__ js, int js_vpb, int js_log, int npad,
                                unsigned *__restrict__ counters, int ncounters) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < ncounters)
-        counters[q] = 0u;
-    float4 out[2];
-    float4 p[2], v[2], f[2];
-#pragma unroll
-    for (int h = 0; h < 2; h++) {  // all loads first (memory-level parallelism)
-        const int i = 2 * q + h;
-        if (i < n) {
-            p[h] = pm[i];
-            v[h] = vel[i];
-            f[h] = force[i];
-        }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ncounters)
+        counters[i] = 0u;
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < n) {
+        float4 pp = pm[i], vv = vel[i];
+        const float4 ff = force[i];
+        const float im = vv.w;
+        vv.x = __fmul_rn(__fadd_rn(vv.x, __fmul_rn(__fmul_rn(ff.x, im), dt)), damping);
+        vv.y = __fmul_rn(__fadd_rn(vv.y, __fmul_rn(__fmul_rn(ff.y, im), dt)), damping);
+        vv.z = __fmul_rn(__fadd_rn(vv.z, __fmul_rn(__fmul_rn(ff.z, im), dt)), damping);
+        pp.x = drift<FUSED_DRIFT>(pp.x, vv.x, dt);
+        pp.y = drift<FUSED_DRIFT>(pp.y, vv.y, dt);
+        pp.z = drift<FUSED_DRIFT>(pp.z, vv.z, dt);
+        pm[i] = pp;
+        vel[i] = vv;
+        out = pp;
     }
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int i = 2 * q + h;
-        if (i < n) {
-            float4 pp = p[h], vv = v[h];
-            const float4 ff = f[h];
-            const float im = vv.w;
-            vv.x = __fmul_rn(__fadd_rn(vv.x, __fmul_rn(__fmul_rn(ff.x, im), dt)), damping);
-            vv.y = __fmul_rn(__fadd_rn(vv.y, __fmul_rn(__fmul_rn(ff.y, im), dt)), damping);
-            vv.z = __fmul_rn(__fadd_rn(vv.z, __fmul_rn(__fmul_rn(ff.z, im), dt)), damping);
-            pp.x = drift<FUSED_DRIFT>(pp.x, vv.x, dt);
-            pp.y = drift<FUSED_DRIFT>(pp.y, vv.y, dt);
-            pp.z = drift<FUSED_DRIFT>(pp.z, vv.z, dt);
-            pm[i] = pp;
-            vel[i] = vv;
-            out[h] = pp;
-        } else {
-            out[h] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-    }
-    if (js && 2 * q < npad)
-        store_jstream(js, js_vpb, js_log, q, out[0], out[1]);
+    if (js)
+        store_jstream_body(js, js_vpb, js_log, i, out, i < npad);
 }
 
-__device__ __forceinline__ double2 ld_d2(const double *p) {
-    return *reinterpret_cast<const double2 *>(p);
-}
-__device__ __forceinline__ void st_d2(double *p, double a, double b) {
-    *reinterpret_cast<double2 *>(p) = make_double2(a, b);
-}
-
-// FP64 kick then drift of bodies 2q, 2q+1: v += a * kick_dt (skipped when
-// kick_dt == 0), x += v * drift_dt; writes x, v, posMass and (js != null)
-// the j-stream pair q.  x64: six SoA components of leading dimension ld
-// (even; entries n..ld-1 are padding).
+// FP64 kick then drift of body i (one per thread): v += a * kick_dt (skipped
+// when kick_dt == 0), x += v * drift_dt; writes x, v, posMass and (js !=
+// null) body i's j-stream entry.  x64: six SoA components of leading
+// dimension ld (entries n..ld-1 are padding, never touched).
 __global__ void __launch_bounds__(kIntegrateThreads)
     kick_drift_kernel(double *__restrict__ x64, size_t ld, const float *__restrict__ mass,
                       const float4 *__restrict__ accel, double kick_dt, double drift_dt, int n,
                       float4 *__restrict__ pm, float4 *__restrict__ js, int js_vpb, int js_log,
                       int npad, unsigned *__restrict__ counters, int ncounters) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < ncounters)
-        counters[q] = 0u;
-    const int i0 = 2 * q;
-    float4 out0 = make_float4(0.f, 0.f, 0.f, 0.f), out1 = out0;
-    if (i0 < n) {
-        const bool two = i0 + 1 < n;
-        double2 X = ld_d2(x64 + i0), Y = ld_d2(x64 + ld + i0), Z = ld_d2(x64 + 2 * ld + i0);
-        double2 U = ld_d2(x64 + 3 * ld + i0), V = ld_d2(x64 + 4 * ld + i0),
-                W = ld_d2(x64 + 5 * ld + i0);
-        const float4 a0 = accel[i0];
-        const float4 a1 = two ? accel[i0 + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
-        float2 m;
-        if (two)
-            m = *reinterpret_cast<const float2 *>(mass + i0);
-        else
-            m = make_float2(mass[i0], 0.f);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ncounters)
+        counters[i] = 0u;
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < n) {
+        double x = x64[i], y = x64[ld + i], z = x64[2 * ld + i];
+        double u = x64[3 * ld + i], v = x64[4 * ld + i], w = x64[5 * ld + i];
+        const float4 a = accel[i];
+        const float m = mass[i];
         if (kick_dt != 0.0) {
-            U.x = fma(widen_f32(a0.x), kick_dt, U.x);
-            V.x = fma(widen_f32(a0.y), kick_dt, V.x);
-            W.x = fma(widen_f32(a0.z), kick_dt, W.x);
-            U.y = fma(widen_f32(a1.x), kick_dt, U.y);
-            V.y = fma(widen_f32(a1.y), kick_dt, V.y);
-            W.y = fma(widen_f32(a1.z), kick_dt, W.y);
+            u = fma(widen_f32(a.x), kick_dt, u);
+            v = fma(widen_f32(a.y), kick_dt, v);
+            w = fma(widen_f32(a.z), kick_dt, w);
         }
-        X.x = fma(U.x, drift_dt, X.x);
-        Y.x = fma(V.x, drift_dt, Y.x);
-        Z.x = fma(W.x, drift_dt, Z.x);
-        X.y = fma(U.y, drift_dt, X.y);
-        Y.y = fma(V.y, drift_dt, Y.y);
-        Z.y = fma(W.y, drift_dt, Z.y);
-        // the padding entry of an odd n is written back as read
-        st_d2(x64 + i0, X.x, X.y);
-        st_d2(x64 + ld + i0, Y.x, Y.y);
-        st_d2(x64 + 2 * ld + i0, Z.x, Z.y);
-        st_d2(x64 + 3 * ld + i0, U.x, U.y);
-        st_d2(x64 + 4 * ld + i0, V.x, V.y);
-        st_d2(x64 + 5 * ld + i0, W.x, W.y);
-        out0 = make_float4(narrow_f64(X.x), narrow_f64(Y.x), narrow_f64(Z.x), m.x);
-        pm[i0] = out0;
-        if (two) {
-            out1 = make_float4(narrow_f64(X.y), narrow_f64(Y.y), narrow_f64(Z.y), m.y);
-            pm[i0 + 1] = out1;
-        }
+        x = fma(u, drift_dt, x);
+        y = fma(v, drift_dt, y);
+        z = fma(w, drift_dt, z);
+        x64[i] = x;
+        x64[ld + i] = y;
+        x64[2 * ld + i] = z;
+        x64[3 * ld + i] = u;
+        x64[4 * ld + i] = v;
+        x64[5 * ld + i] = w;
+        out = make_float4(narrow_f64(x), narrow_f64(y), narrow_f64(z), m);
+        pm[i] = out;
     }
-    if (js && i0 < npad)
-        store_jstream(js, js_vpb, js_log, q, out0, out1);
+    if (js)
+        store_jstream_body(js, js_vpb, js_log, i, out, i < npad);
 }
 
-// FP64 kick of bodies 2q, 2q+1: v += a * kick_dt.
+// FP64 kick of body i (one per thread): v += a * kick_dt.
 __global__ void __launch_bounds__(kIntegrateThreads)
     half_kick_kernel(double *__restrict__ x64, size_t ld, const float4 *__restrict__ accel,
                      double kick_dt, int n) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i0 = 2 * q;
-    if (i0 >= n)
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
         return;
-    const bool two = i0 + 1 < n;
-    double *u = x64 + 3 * ld + i0, *v = x64 + 4 * ld + i0, *w = x64 + 5 * ld + i0;
-    double2 U = ld_d2(u), V = ld_d2(v), W = ld_d2(w);
-    const float4 a0 = accel[i0];
-    const float4 a1 = two ? accel[i0 + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
-    U.x = fma(widen_f32(a0.x), kick_dt, U.x);
-    V.x = fma(widen_f32(a0.y), kick_dt, V.x);
-    W.x = fma(widen_f32(a0.z), kick_dt, W.x);
-    U.y = fma(widen_f32(a1.x), kick_dt, U.y);
-    V.y = fma(widen_f32(a1.y), kick_dt, V.y);
-    W.y = fma(widen_f32(a1.z), kick_dt, W.y);
-    st_d2(u, U.x, U.y);
-    st_d2(v, V.x, V.y);
-    st_d2(w, W.x, W.y);
+    double *u = x64 + 3 * ld + i, *v = x64 + 4 * ld + i, *w = x64 + 5 * ld + i;
+    // every load before the first store (the three components are one
+    // array to the compiler, which would otherwise order each load after the
+    // previous component's store: three memory round trips instead of one)
+    const double u0 = *u, v0 = *v, w0 = *w;
+    const float4 a = accel[i];
+    *u = fma(widen_f32(a.x), kick_dt, u0);
+    *v = fma(widen_f32(a.y), kick_dt, v0);
+    *w = fma(widen_f32(a.z), kick_dt, w0);
 }
 
 static inline unsigned blocks_for(int work) {
@@ -217,8 +153,7 @@ int launch_integrate_reference(float4 *pm, float4 *vel, const float4 *force, flo
                                float damping, size_t n, int fused_drift, float4 *js, int js_vpb,
                                int js_log, int npad, unsigned *counters, int ncounters,
                                cudaStream_t st) {
-    const int pairs = (int)((n + 1) / 2);
-    const int work = std::max(std::max(pairs, npad / 2), ncounters);
+    const int work = std::max(std::max((int)n, npad), ncounters);
     if (fused_drift)
         integrate_reference_kernel<true><<<blocks_for(work), kIntegrateThreads, 0, st>>>(
             pm, vel, force, dt, damping, (int)n, js, js_vpb, js_log, npad, counters, ncounters);
@@ -234,8 +169,7 @@ int launch_kick_drift(double *x64, size_t ld, const float *mass, const float4 *a
                       cudaStream_t st) {
     if ((ld & 1) || ld < n)
         return NBGB_ERR_INVALID_ARGUMENT;
-    const int pairs = (int)((n + 1) / 2);
-    const int work = std::max(std::max(pairs, npad / 2), ncounters);
+    const int work = std::max(std::max((int)n, npad), ncounters);
     kick_drift_kernel<<<blocks_for(work), kIntegrateThreads, 0, st>>>(
         x64, ld, mass, accel, kick_dt, drift_dt, (int)n, pm, js, js_vpb, js_log, npad, counters,
         ncounters);
@@ -246,9 +180,8 @@ int launch_half_kick(double *x64, size_t ld, const float4 *accel, double kick_dt
                      cudaStream_t st) {
     if ((ld & 1) || ld < n)
         return NBGB_ERR_INVALID_ARGUMENT;
-    const int pairs = (int)((n + 1) / 2);
-    half_kick_kernel<<<blocks_for(pairs), kIntegrateThreads, 0, st>>>(x64, ld, accel, kick_dt,
-                                                                      (int)n);
+    half_kick_kernel<<<blocks_for((int)n), kIntegrateThreads, 0, st>>>(x64, ld, accel, kick_dt,
+                                                                        (int)n);
     return cudaGetLastError() == cudaSuccess ? NBGB_OK : NBGB_ERR_CUDA;
 }
 

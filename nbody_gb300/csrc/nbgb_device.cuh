@@ -199,6 +199,39 @@ __device__ __forceinline__ float jstream_log_mass(float m) {
     return __int_as_float(0x7fc00000);  // NaN
 }
 
+// Body i's entry of the j-stream, written by the thread that owns body i (one
+// body per thread, consecutive threads on consecutive bodies, so every load
+// and store of the caller is coalesced).  Paired layout (vpb 1): lanes i and
+// i ^ 1 (one warp: blocks are whole warps and i is the thread's global
+// index) swap their bodies, the even lane stores float4 2q = {x0,x1,y0,y1}
+// and the odd lane 2q+1 = {z0,z1,m0,m1}; duplicated layout (vpb 2): each
+// lane stores its body's {x,x,y,y}, {z,z,m,m}.  logm: pair q % 4 == 0 holds
+// log2 of the masses.  Every lane of the warp calls it (shuffles); lanes with
+// in_range false (beyond the padded length) store nothing.
+__device__ __forceinline__ void store_jstream_body(float4 *__restrict__ js, int vpb, int logm,
+                                                   int i, float4 b, bool in_range) {
+    const int q = i >> 1;
+    if (logm && jstream_log_slot(q))
+        b.w = jstream_log_mass(b.w);
+    if (vpb == 2) {
+        if (in_range) {
+            js[2 * i] = make_float4(b.x, b.x, b.y, b.y);
+            js[2 * i + 1] = make_float4(b.z, b.z, b.w, b.w);
+        }
+        return;
+    }
+    const float ox = __shfl_xor_sync(0xffffffffu, b.x, 1);
+    const float oy = __shfl_xor_sync(0xffffffffu, b.y, 1);
+    const float oz = __shfl_xor_sync(0xffffffffu, b.z, 1);
+    const float ow = __shfl_xor_sync(0xffffffffu, b.w, 1);
+    if (!in_range)
+        return;
+    if ((i & 1) == 0)
+        js[2 * q] = make_float4(b.x, ox, b.y, oy);
+    else
+        js[2 * q + 1] = make_float4(oz, b.z, ow, b.w);
+}
+
 // One interaction, scalar FP32 pipe.
 __device__ __forceinline__ void pair_interact1(float sx, float sy, float sz, float sm,
                                                float x, float y, float z, float eps2,
